@@ -1,0 +1,300 @@
+"""ctypes front end of the test oracle -- TEST INFRASTRUCTURE ONLY.
+
+PortSim     -- the CPU restatement (ubg_oracle.c), REAL=float or REAL=double.
+RefSim      -- the reference's own Simulation (simulation.cpp,
+               pressure_solver.cpp of te42kyfo/ubootgl) built by
+               ref/build_ref.py; present only where that build can run
+               (x86-64 with the reference checkout).
+Both expose the same methods, so tests can swap one for the other.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+FIELD = {"vx": 0, "vy": 1, "vx_back": 2, "vy_back": 3, "p": 4, "f": 5, "flag": 6,
+         "vx_accum": 7, "vy_accum": 8}
+
+_port = None
+_ref = None
+
+
+def _fp(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def port_lib():
+    global _port
+    if _port is None:
+        lib = C.CDLL(build_oracle.build())
+        for sfx, ct in (("f", C.c_float), ("d", C.c_double)):
+            P = C.POINTER(ct)
+            g = lambda n: getattr(lib, "ubo_%s_%s" % (sfx, n))
+            g("create").restype = C.c_void_p
+            g("create").argtypes = [P, C.c_int, C.c_int, ct, ct]
+            g("destroy").argtypes = [C.c_void_p]
+            for n in ("step",):
+                g(n).argtypes = [C.c_void_p, ct]
+            g("step_ncycles").argtypes = [C.c_void_p, ct, C.c_int]
+            g("set_dt").argtypes = [C.c_void_p, ct]
+            for n in ("apply_accum", "diffuse", "advect", "set_vbcs", "set_pbc", "project"):
+                g(n).argtypes = [C.c_void_p]
+            g("project_ncycles").argtypes = [C.c_void_p, C.c_int]
+            g("sim_mg_solve").argtypes = [C.c_void_p, C.c_int]
+            g("get_field").argtypes = [C.c_void_p, C.c_int, P]
+            g("set_field").argtypes = [C.c_void_p, C.c_int, P]
+            g("update_flag").argtypes = [C.c_void_p, P]
+            g("get_h").restype = ct
+            g("get_h").argtypes = [C.c_void_p]
+            g("mg_levels").argtypes = [C.c_void_p]
+            g("mg_level_flag").argtypes = [C.c_void_p, C.c_int, P]
+            g("mg_level_size").argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int)]
+            g("add_sink").argtypes = [C.c_void_p, ct, ct, ct]
+            g("mg_create").restype = C.c_void_p
+            g("mg_create").argtypes = [C.c_int, C.c_int, P]
+            g("mg_destroy").argtypes = [C.c_void_p]
+            g("mg_nlevels").argtypes = [C.c_void_p]
+            g("mg_solve").argtypes = [C.c_void_p, P, P, P, ct, C.c_int]
+            g("rbgs").argtypes = [P, P, P, C.c_int, C.c_int, ct, ct]
+            g("residual").restype = C.c_double
+            g("residual").argtypes = [P, P, P, P, C.c_int, C.c_int, ct]
+            g("advect_mask_vx").argtypes = [P, C.c_int, C.c_int, C.c_int]
+            g("advect_mask_vy").argtypes = [P, C.c_int, C.c_int, C.c_int]
+        lib.ubo_omp_set_threads.argtypes = [C.c_int]
+        if hasattr(lib, "ubo_tracers_f_step"):
+            _bind_tracers(lib)
+        _port = lib
+    return _port
+
+
+def _bind_tracers(lib):
+    P = C.POINTER(C.c_float)
+    U = C.POINTER(C.c_uint32)
+    lib.ubo_tracers_f_step.argtypes = [P, P, C.c_int, C.c_int, P, C.c_int, P, C.c_int,
+                                       C.c_int, U, U, P, C.c_float, C.c_float, C.c_uint32]
+    lib.ubo_velocity_texture_f.argtypes = [P, P, C.c_int, C.c_int, P, P]
+
+
+def ref_available():
+    from .ref import build_ref
+    return build_ref.available()
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        from .ref import build_ref
+        lib = C.CDLL(build_ref.build())
+        P = C.POINTER(C.c_float)
+        lib.ref_create.restype = C.c_void_p
+        lib.ref_create.argtypes = [P, C.c_int, C.c_int, C.c_float, C.c_float]
+        lib.ref_destroy.argtypes = [C.c_void_p]
+        lib.ref_set_field.argtypes = [C.c_void_p, C.c_int, P]
+        lib.ref_get_field.argtypes = [C.c_void_p, C.c_int, P]
+        lib.ref_update_flag.argtypes = [C.c_void_p, P]
+        lib.ref_get_h.restype = C.c_float
+        lib.ref_get_h.argtypes = [C.c_void_p]
+        lib.ref_set_dt.argtypes = [C.c_void_p, C.c_float]
+        lib.ref_step.argtypes = [C.c_void_p, C.c_float]
+        for n in ("apply_accum", "diffuse", "advect", "set_vbcs", "set_pbc", "project"):
+            getattr(lib, "ref_" + n).argtypes = [C.c_void_p]
+        lib.ref_mg_solve_sim.argtypes = [C.c_void_p, C.c_int]
+        lib.ref_add_sink.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float]
+        lib.ref_mg_create.restype = C.c_void_p
+        lib.ref_mg_create.argtypes = [C.c_int, C.c_int, P]
+        lib.ref_mg_destroy.argtypes = [C.c_void_p]
+        lib.ref_mg_solve.argtypes = [C.c_void_p, P, P, P, C.c_int, C.c_int, C.c_float, C.c_int]
+        lib.ref_rbgs.argtypes = [P, P, P, C.c_int, C.c_int, C.c_float]
+        lib.ref_residual.restype = C.c_float
+        lib.ref_residual.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_float]
+        lib.ref_set_threads.argtypes = [C.c_int]
+        _ref = lib
+    return _ref
+
+
+def field_shape(name, W, H):
+    if name in ("vx", "vx_back", "vx_accum"):
+        return (H, W - 1)
+    if name in ("vy", "vy_back", "vy_accum"):
+        return (H - 1, W)
+    return (H, W)
+
+
+class PortSim:
+    """The CPU restatement's Simulation (dtype float32 or float64)."""
+
+    def __init__(self, flag, pwidth=1.0, mu=1e-4, dtype=np.float32):
+        self.lib = port_lib()
+        self.dtype = np.dtype(dtype)
+        self.sfx = "f" if self.dtype == np.float32 else "d"
+        self.ct = C.c_float if self.sfx == "f" else C.c_double
+        flag = np.ascontiguousarray(flag, dtype=self.dtype)
+        self.H, self.W = flag.shape
+        self.h_ = self._fn("create")(_fp(flag, self.ct), self.W, self.H, pwidth, mu)
+        if not self.h_:
+            raise ValueError("oracle create failed")
+
+    def _fn(self, n):
+        return getattr(self.lib, "ubo_%s_%s" % (self.sfx, n))
+
+    def __del__(self):
+        if getattr(self, "h_", None):
+            self._fn("destroy")(self.h_)
+            self.h_ = None
+
+    @property
+    def h(self):
+        return self._fn("get_h")(self.h_)
+
+    def get(self, name):
+        out = np.empty(field_shape(name, self.W, self.H), dtype=self.dtype)
+        self._fn("get_field")(self.h_, FIELD[name], _fp(out, self.ct))
+        return out
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        assert a.shape == field_shape(name, self.W, self.H), (name, a.shape)
+        self._fn("set_field")(self.h_, FIELD[name], _fp(a, self.ct))
+
+    def update_flag(self, flag):
+        a = np.ascontiguousarray(flag, dtype=self.dtype)
+        self._fn("update_flag")(self.h_, _fp(a, self.ct))
+
+    def step(self, dt, ncycles=2):
+        self._fn("step_ncycles")(self.h_, dt, ncycles)
+
+    def set_dt(self, dt):
+        self._fn("set_dt")(self.h_, dt)
+
+    def stage(self, name):
+        self._fn(name)(self.h_)
+
+    def mg_solve(self, zgbc=True):
+        self._fn("sim_mg_solve")(self.h_, 1 if zgbc else 0)
+
+    def add_sink(self, x, y, z):
+        self._fn("add_sink")(self.h_, x, y, z)
+
+    def levels(self):
+        return self._fn("mg_levels")(self.h_)
+
+    def level_flag(self, level):
+        w, h = C.c_int(), C.c_int()
+        self._fn("mg_level_size")(self.h_, level, C.byref(w), C.byref(h))
+        out = np.empty((h.value, w.value), dtype=self.dtype)
+        self._fn("mg_level_flag")(self.h_, level, _fp(out, self.ct))
+        return out
+
+
+class RefSim:
+    """The reference's own Simulation, compiled from its sources (float32)."""
+
+    def __init__(self, flag, pwidth=1.0, mu=1e-4, threads=None):
+        self.lib = ref_lib()
+        flag = np.ascontiguousarray(flag, dtype=np.float32)
+        self.H, self.W = flag.shape
+        self.dtype = np.dtype(np.float32)
+        self.set_threads(threads)
+        self.h_ = self.lib.ref_create(_fp(flag, C.c_float), self.W, self.H, pwidth, mu)
+
+    def set_threads(self, threads=None):
+        # Classic (deterministic) red-black schedule needs H/threads < 100 at
+        # every level with H >= 20 (pressure_solver.cpp:52, 65).
+        if threads is None:
+            threads = max(1, self.H // 100 + 1)
+        self.lib.ref_set_threads(threads)
+
+    def __del__(self):
+        if getattr(self, "h_", None):
+            self.lib.ref_destroy(self.h_)
+            self.h_ = None
+
+    @property
+    def h(self):
+        return self.lib.ref_get_h(self.h_)
+
+    def get(self, name):
+        out = np.empty(field_shape(name, self.W, self.H), dtype=np.float32)
+        self.lib.ref_get_field(self.h_, FIELD[name], _fp(out, C.c_float))
+        return out
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        assert a.shape == field_shape(name, self.W, self.H), (name, a.shape)
+        self.lib.ref_set_field(self.h_, FIELD[name], _fp(a, C.c_float))
+
+    def update_flag(self, flag):
+        a = np.ascontiguousarray(flag, dtype=np.float32)
+        self.lib.ref_update_flag(self.h_, _fp(a, C.c_float))
+
+    def step(self, dt, ncycles=2):
+        assert ncycles == 2, "the reference always runs two V-cycles"
+        self.lib.ref_step(self.h_, dt)
+
+    def set_dt(self, dt):
+        self.lib.ref_set_dt(self.h_, dt)
+
+    def stage(self, name):
+        getattr(self.lib, "ref_" + name)(self.h_)
+
+    def mg_solve(self, zgbc=True):
+        self.lib.ref_mg_solve_sim(self.h_, 1 if zgbc else 0)
+
+    def add_sink(self, x, y, z):
+        self.lib.ref_add_sink(self.h_, x, y, z)
+
+
+def port_mg_solve(p, f, flag, h, zgbc=False, coarse_flag=None, dtype=np.float32):
+    """Standalone MG::solve on copies (class MG, pressure_solver.hpp:13-76).
+    coarse_flag=None builds MG(width, height) (all coarse flags 1.0, as
+    mgtest does); otherwise MG(coarse_flag)."""
+    lib = port_lib()
+    sfx = "f" if np.dtype(dtype) == np.float32 else "d"
+    ct = C.c_float if sfx == "f" else C.c_double
+    g = lambda n: getattr(lib, "ubo_%s_%s" % (sfx, n))
+    Hh, Ww = p.shape
+    pp = np.ascontiguousarray(p, dtype=dtype).copy()
+    ff = np.ascontiguousarray(f, dtype=dtype)
+    fl = np.ascontiguousarray(flag, dtype=dtype)
+    cf = None if coarse_flag is None else np.ascontiguousarray(coarse_flag, dtype=dtype)
+    mg = g("mg_create")(Ww, Hh, None if cf is None else _fp(cf, ct))
+    try:
+        g("mg_solve")(mg, _fp(pp, ct), _fp(ff, ct), _fp(fl, ct), h, 1 if zgbc else 0)
+    finally:
+        g("mg_destroy")(mg)
+    return pp
+
+
+def ref_mg_solve(p, f, flag, h, zgbc=False, coarse_flag=None, threads=None):
+    lib = ref_lib()
+    Hh, Ww = p.shape
+    lib.ref_set_threads(threads or max(1, Hh // 100 + 1))
+    pp = np.ascontiguousarray(p, dtype=np.float32).copy()
+    ff = np.ascontiguousarray(f, dtype=np.float32)
+    fl = np.ascontiguousarray(flag, dtype=np.float32)
+    cf = None if coarse_flag is None else np.ascontiguousarray(coarse_flag, dtype=np.float32)
+    mg = lib.ref_mg_create(Ww, Hh, None if cf is None else _fp(cf, C.c_float))
+    try:
+        lib.ref_mg_solve(mg, _fp(pp, C.c_float), _fp(ff, C.c_float), _fp(fl, C.c_float), Ww, Hh,
+                         h, 1 if zgbc else 0)
+    finally:
+        lib.ref_mg_destroy(mg)
+    return pp
+
+
+def port_residual(p, f, flag, h, dtype=np.float32):
+    lib = port_lib()
+    sfx = "f" if np.dtype(dtype) == np.float32 else "d"
+    ct = C.c_float if sfx == "f" else C.c_double
+    Hh, Ww = p.shape
+    a = [np.ascontiguousarray(x, dtype=dtype) for x in (p, f, flag)]
+    r = np.zeros((Hh, Ww), dtype=dtype)
+    n = getattr(lib, "ubo_%s_residual" % sfx)(*[_fp(x, ct) for x in a], _fp(r, ct), Ww, Hh, h)
+    return r, n
+
+
+def set_threads(n):
+    port_lib().ubo_omp_set_threads(n)

@@ -1,0 +1,107 @@
+"""Seeded synthetic workloads for the ubootgl fluid step.
+
+The reference's game builds its flag mask from a level PNG
+(terrain.cpp:20-49) and its velocity from the simulation's constructor
+(simulation.hpp:32-67).  Benchmarks and tests here use seeded synthetic
+stand-ins with the shapes the step is quoted on:
+
+* flag: 1 = fluid, 0 = solid; solid rows y = 0 and y = H-1 (no-slip walls),
+  fluid inflow column x = 0 and outflow column x = W-1, plus seeded solid
+  discs.  Values are exactly 0.0 or 1.0, like Terrain::subSample's output
+  (terrain.cpp:3-11).
+* velocity: vx = 1 + 0.1*n1, vy = 0.1*n2 with n1, n2 Gaussian-smoothed
+  (sigma = 8 cells) white noise normalised to unit standard deviation; faces
+  touching a solid cell are zeroed (the rule of Simulation::setGrids,
+  simulation.hpp:82-98); inflow vx(0, y) = u_in on fluid rows.
+* time step: dt = cfl * h / max|u| with cfl = 0.5, computed by the caller
+  from the current fields.
+"""
+import math
+
+import numpy as np
+
+
+def disc_flag(W, H, n_discs=12, r_range=(20, 60), seed=0, solid_frac=None):
+    """Channel with solid top/bottom rows and seeded solid discs.
+
+    r_range is in cells for W = 1024 and scales with W / 1024, so the same
+    flow set-up holds at every size.  With solid_frac, discs are added
+    (rejection-free, one at a time) until the solid fraction reaches it.
+    """
+    rng = np.random.default_rng(seed)
+    flag = np.ones((H, W), dtype=np.float32)
+    flag[0, :] = 0.0
+    flag[H - 1, :] = 0.0
+    scale = W / 1024.0
+    rmin, rmax = r_range[0] * scale, r_range[1] * scale
+    yy, xx = np.mgrid[0:H, 0:W]
+
+    def add_disc():
+        r = rng.uniform(rmin, rmax)
+        cx = rng.uniform(0.1 * W + r, 0.95 * W - r) if 0.85 * W > 2 * r else 0.5 * W
+        cy = rng.uniform(r, H - r) if H > 2 * r else 0.5 * H
+        y0, y1 = max(1, int(cy - r) - 1), min(H - 1, int(cy + r) + 2)
+        x0, x1 = max(1, int(cx - r) - 1), min(W - 1, int(cx + r) + 2)
+        sub = (xx[y0:y1, x0:x1] - cx) ** 2 + (yy[y0:y1, x0:x1] - cy) ** 2 <= r * r
+        flag[y0:y1, x0:x1][sub] = 0.0
+
+    if solid_frac is None:
+        for _ in range(n_discs):
+            add_disc()
+    else:
+        guard = 0
+        while 1.0 - flag.mean() < solid_frac and guard < 100000:
+            add_disc()
+            guard += 1
+    return flag
+
+
+def _smooth_noise(rng, shape, sigma):
+    from scipy.ndimage import gaussian_filter
+
+    n = rng.standard_normal(shape).astype(np.float64)
+    n = gaussian_filter(n, sigma=sigma, mode="wrap")
+    s = n.std()
+    return (n / (s if s > 0 else 1.0)).astype(np.float32)
+
+
+def initial_velocity(flag, seed=1, amp=0.1, sigma=8.0, u_in=1.0):
+    """Return (vx, vy) with shapes (H, W-1) and (H-1, W)."""
+    H, W = flag.shape
+    rng = np.random.default_rng(seed)
+    vx = (1.0 + amp * _smooth_noise(rng, (H, W - 1), sigma)).astype(np.float32)
+    vy = (amp * _smooth_noise(rng, (H - 1, W), sigma)).astype(np.float32)
+    vx[:, 0] = u_in
+    vx[:, :] *= flag[:, :-1] * flag[:, 1:]
+    vy[:, :] *= flag[:-1, :] * flag[1:, :]
+    vy[0, :] = 0.0
+    return np.ascontiguousarray(vx), np.ascontiguousarray(vy)
+
+
+def cfl_dt(vx, vy, h, cfl=0.5):
+    """dt = cfl * h / max|u| over both staggered components (float32)."""
+    umax = max(float(np.abs(vx).max()), float(np.abs(vy).max()), 1e-7)
+    return np.float32(cfl * h / umax)
+
+
+def grid_h(W, pwidth=1.0):
+    """Simulation::h = pwidth / (width - 1.0f) (simulation.hpp:63), in float32."""
+    return float(np.float32(pwidth) / (np.float32(W) - np.float32(1.0)))
+
+
+def mg_levels(W, H):
+    """Level sizes of MG(width, height), pressure_solver.hpp:16-31."""
+    out = []
+    while W > 3 and H > 3:
+        out.append((W, H))
+        W //= 2
+        H //= 2
+    return out
+
+
+def batch_sizes(n, wmin=128, wmax=2048, seed=0, multiple=32):
+    """Widths log-uniform in [wmin, wmax] rounded to `multiple`, height = w/2."""
+    rng = np.random.default_rng(seed)
+    ws = np.exp(rng.uniform(math.log(wmin), math.log(wmax), size=n))
+    ws = np.clip((np.round(ws / multiple) * multiple).astype(int), wmin, wmax)
+    return [(int(w), int(w) // 2) for w in ws]
