@@ -1,0 +1,411 @@
+"""Benchmark of the ubootgl fluid step on one GB300.
+
+Workload (the metric's configuration): one 4096 x 2048 staggered-MAC grid,
+float32 u/v/p, uint8 flag; solid top/bottom walls plus 12 seeded solid
+discs (radius 20-60 cells at W = 1024, scaled to W); inflow u = 1.0;
+initial velocity 1.0 + 0.1 * Gaussian-smoothed (sigma 8) noise; mu = 1e-4;
+dt = 0.5 h / max|u| computed on the device every step.  A "step" is
+Simulation::step (simulation.cpp:356-374): diffusion, bicubic
+semi-Lagrangian advection, projection with the reference's two multigrid
+V-cycles, boundary conditions.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is whole-job Mcell-steps/s with all fields
+resident in HBM; `e2e` is the same metric through the C ABI with host
+buffers (each step uploads vx, vy from pinned host memory and downloads the
+display fields vx_current, vy_current).  The reference arm times the CPU
+step on the host cores (see --impl reference).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_DEFAULT, H_DEFAULT = 4096, 2048
+METRIC = "Mcell-steps/s at 4096x2048 (FP32, reference step: 2 V-cycles)"
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def workload(W, H, seed=2024):
+    from ubootgl_gb300 import workload as WL
+    flag = WL.disc_flag(W, H, n_discs=12, r_range=(20, 60), seed=seed)
+    vx, vy = WL.initial_velocity(flag, seed=seed + 1)
+    return flag, vx, vy
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def time_cpu_step(W, H, budget_s=20.0, min_steps=3, max_steps=None, threads=None):
+    """The reference step on the host cores: oracle/_ref (the reference's own
+    simulation.cpp built from source) where it builds (x86-64), else the C
+    restatement of it.  Returns (Mcell-steps/s, info)."""
+    from oracle import oracle as O
+    flag, vx, vy = workload(W, H)
+    threads = threads or cpu_threads()
+    kind = "port"
+    sim = None
+    try:
+        if O.ref_available():
+            # the classic (deterministic) red-black schedule needs H/T < 100
+            sim = O.RefSim(flag, threads=max(threads, H // 100 + 1))
+            kind = "reference"
+    except Exception:
+        sim = None
+    if sim is None:
+        O.set_threads(threads)
+        sim = O.PortSim(flag)
+    for n in ("vx", "vy", "vx_back", "vy_back"):
+        sim.set(n, vx if n.startswith("vx") else vy)
+    from ubootgl_gb300 import workload as WL
+    h = sim.h
+    # warm-up step
+    sim.step(WL.cfl_dt(sim.get("vx"), sim.get("vy"), h))
+    n, t_total = 0, 0.0
+    while True:
+        dt = WL.cfl_dt(sim.get("vx"), sim.get("vy"), h)
+        t0 = time.perf_counter()
+        sim.step(dt)
+        t_total += time.perf_counter() - t0
+        n += 1
+        if (n >= min_steps and t_total >= budget_s) or (max_steps and n >= max_steps):
+            break
+    val = W * H * n / t_total / 1e6
+    return val, {"kind": kind, "cores": threads, "steps": n, "seconds": t_total,
+                 "sample": "%dx%d full steps (2 V-cycles), %d timed after 1 warm-up; "
+                           "dt = 0.5 h/max|u| computed outside the timed call" % (W, H, n)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    W, H = args.width, args.height
+    steps = max(1, args.steps)
+    # each timed step is one full CPU step of the workload; the number of
+    # timed steps is bounded so that the run ends within a few minutes
+    val, info = time_cpu_step(W, H, budget_s=30.0, min_steps=1, max_steps=min(steps, 200))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "Mcell-steps/s",
+        "n_gpus": args.gpus, "steps": info["steps"], "warmup": 1,
+        "ms_per_step": round(1e3 * info["seconds"] / info["steps"], 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded disc mask + smoothed-noise velocity)",
+        "config": {"workload": "fluid step %dx%d, 12 discs, 2 V-cycles" % (W, H),
+                   "parallelism": "host cores"},
+        "cpu_baseline": {"value": round(val, 3), "unit": "Mcell-steps/s", "cores": info["cores"],
+                         "kind": info["kind"], "sample": info["sample"]},
+        "e2e": {"value": round(val, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    if info["kind"] == "port":
+        line["note"] = ("the reference's step uses x86 AVX2 intrinsics (interpolators.hpp) and "
+                        "does not build on this aarch64 host; its C restatement is timed instead")
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes as C
+
+    rank, world, local = dist_env()
+    from ubootgl_gb300 import _lib as L
+    from ubootgl_gb300.simulation import Simulation
+
+    lib = L.load()
+    W, H = args.width, args.height
+    flag, vx, vy = workload(W, H, seed=2024 + rank)
+    sim = Simulation(flag, 1.0, 1e-4)
+    sim.set("vx", vx)
+    sim.set("vy", vy)
+    sim.set("vx_back", vx)
+    sim.set("vy_back", vy)
+    stream = C.c_void_p()
+    L.check(lib.ubg_stream(sim._h, C.byref(stream)))
+
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    ext_stream = torch.cuda.ExternalStream(stream.value, device=dev)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    for _ in range(args.warmup):
+        sim.step_cfl(0.5)
+    sim.sync()
+
+    # ---- timed region: K steps, fields resident in HBM
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    sim.sync()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(ext_stream)
+    for _ in range(args.steps):
+        sim.step_cfl(0.5)
+    ev1.record(ext_stream)
+    sim.sync()
+    barrier()
+    clk = clocks.stop()
+    prof = sim.profile_read()
+    ms = ev0.elapsed_time(ev1)
+    if pg:
+        t = torch.tensor([ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    cells = W * H
+    value = cells * args.steps * world / (ms / 1e3) / 1e6
+    launches_per_step = prof["kernel_launches"]
+
+    # ---- dominant kernel timing (CUDA events on the handle's stream)
+    kt = kernel_timing(sim, lib, W, H, reps=args.profile_steps)
+
+    # ---- end-to-end through the C ABI with host buffers
+    e2e = end_to_end(sim, L, lib, W, H, max(3, min(args.steps, args.e2e_steps)), barrier, pg,
+                     world, dev)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "Mcell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded disc mask + smoothed-noise velocity)",
+        "config": {"workload": "fluid step %dx%d, 12 discs, FP32, 2 V-cycles, dt=0.5h/max|u| on device"
+                               % (W, H),
+                   "grid": [W, H], "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2: step working set %.0f MB > 129 MB"
+                         % (working_set_bytes(W, H) / 1e6)},
+        "clocks": clk,
+        "gpu_launches": int(launches_per_step * args.steps),
+        "e2e": e2e,
+        "roofline": kt["roofline"],
+        "kernels": kt["detail"],
+        "profiled_step_ms": kt["profiled_step_ms"],
+    }
+    if not args.no_cpu_baseline:
+        val, info = time_cpu_step(W, H, budget_s=args.cpu_budget)
+        line["cpu_baseline"] = {"value": round(val, 3), "unit": "Mcell-steps/s",
+                                "cores": info["cores"], "kind": info["kind"],
+                                "sample": info["sample"]}
+    print(json.dumps(line), flush=True)
+
+
+def working_set_bytes(W, H):
+    n = W * H
+    return n * (4 * 4 + 4 * 2 + 4 * 2 + 1) * 4 // 3 + n * 4 * 2
+
+
+# Algorithmic bytes per cell of each kernel class (FP32 fields, uint8 flag,
+# every input read once and every output written once), per launch.  The
+# level-0 smoother does 3 red-black sweeps per launch; its figure is the
+# unfused per-sweep 13 B/cell (read p, f, flag; write p) times 3.
+ALG_BYTES_PER_CELL = {
+    "smooth_l0": 3 * 13.0,
+    "resid_restrict_l0": 9.0 + 1.0,     # read p, f, flag; write rc (1/4 cell)
+    "diffuse": 2 * (4 + 4 + 1),         # one sweep of vx and vy
+    "advect": 2 * 4 + 1 + 2 * 4,        # read vx, vy, flag; write vx, vy
+    "divergence": 8 + 4,
+    "gradient": 4 + 1 + 8 + 8,
+}
+
+
+def kernel_timing(sim, lib, W, H, reps=30):
+    """Per-kernel durations from CUDA events on the simulation's stream,
+    recorded around every launch of `reps` further steps (direct launches:
+    profiling mode does not use the step graph)."""
+    sim.profile(True)
+    sim.profile_reset()
+    for _ in range(reps):
+        sim.step_cfl(0.5)
+    sim.sync()
+    classes = sim.profile_classes()
+    step_ms = sim.profile_read()["step_ms"]
+    sim.profile(False)
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    if not peak:
+        peak, peak_src = 6800.0, "fallback"
+    cells = W * H
+    total = sum(v[0] for v in classes.values()) or 1.0
+    detail = {}
+    for name, (ms, n) in sorted(classes.items(), key=lambda kv: -kv[1][0]):
+        d = {"share": round(ms / total, 4), "launches_per_step": round(n / reps, 2),
+             "mean_ms": round(ms / n, 5)}
+        if name in ALG_BYTES_PER_CELL:
+            gbs = ALG_BYTES_PER_CELL[name] * cells / (ms / n / 1e3) / 1e9
+            d["alg_gbs"] = round(gbs, 1)
+        detail[name] = d
+    dom = "smooth_l0"
+    ms_l = classes[dom][0] / classes[dom][1]
+    alg = ALG_BYTES_PER_CELL[dom] * cells
+    compulsory = 13.0 * cells
+    achieved = alg / (ms_l / 1e3) / 1e9
+    ach_c = compulsory / (ms_l / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_smooth level 0 (3 red-black sweeps per launch, "
+                                      "temporally blocked in shared memory)",
+            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 3), "peak_source": peak_src,
+            "traffic": None, "launch_ms": round(ms_l, 5),
+            "alg_bytes_per_launch": alg,
+            "achieved_compulsory": round(ach_c, 1),
+            "frac_compulsory": round(ach_c / peak, 3),
+            "compulsory_bytes_per_launch": compulsory}
+    return {"roofline": roof, "detail": detail, "profiled_step_ms": round(step_ms, 4)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def end_to_end(sim, L, lib, W, H, steps, barrier, pg, world, dev):
+    """Same metric through the public C ABI with host buffers: per step the
+    velocity state goes host -> device from pinned memory, the step runs, and
+    the display fields (vx_current, vy_current) come back device -> host."""
+    import torch
+    hx = L.PinnedArray((H, W - 1))
+    hy = L.PinnedArray((H - 1, W))
+    ox = L.PinnedArray((H, W - 1))
+    oy = L.PinnedArray((H - 1, W))
+    hx.array[:] = sim.get("vx")
+    hy.array[:] = sim.get("vy")
+    fx, fy = L.FIELDS["vx"], L.FIELDS["vy"]
+    cx, cy = L.FIELDS["vx_current"], L.FIELDS["vy_current"]
+
+    def one():
+        L.check(lib.ubg_upload(sim._h, fx, L.fptr(hx.array)))
+        L.check(lib.ubg_upload(sim._h, fy, L.fptr(hy.array)))
+        sim.step_cfl(0.5)
+        L.check(lib.ubg_download(sim._h, cx, L.fptr(ox.array)))
+        L.check(lib.ubg_download(sim._h, cy, L.fptr(oy.array)))
+
+    for _ in range(3):
+        one()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    t1 = time.perf_counter()
+    barrier()
+    sec = t1 - t0
+    if pg:
+        t = torch.tensor([sec], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        sec = float(t.item())
+    val = W * H * steps * world / sec / 1e6
+    b_in = 4 * ((W - 1) * H + W * (H - 1))
+    return {"value": round(val, 2), "unit": "Mcell-steps/s", "h2d_bytes_per_step": b_in,
+            "d2h_bytes_per_step": b_in, "steps": steps,
+            "ms_per_step": round(1e3 * sec / steps, 4)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=W_DEFAULT)
+    ap.add_argument("--height", type=int, default=H_DEFAULT)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=30)
+    ap.add_argument("--e2e-steps", type=int, default=200)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+/*
+ * ubootgl_gb300 -- C ABI of the GB300 (sm_103a) fluid step.
+ *
+ * This is the drop-in boundary for ubootgl's hot path: the 2-D staggered-MAC
+ * fluid time step `Simulation::step` (simulation.cpp:356-374) and its
+ * multigrid pressure solver `class MG` (pressure_solver.hpp:13-76) of
+ * te42kyfo/ubootgl.  Each entry point below names the reference interface it
+ * replaces.  The C++ classes in ubootgl_gb300/simulation.hpp wrap these calls
+ * with the reference's own class and method names.
+ *
+ * Conventions
+ *  - Grids are row-major, element (x, y) at y*width + x, exactly as
+ *    Single2DGrid / DoubleBuffered2DGrid (db2dgrid.hpp:12-108).  For a
+ *    simulation of width W and height H: p, f, flag are W x H; vx is
+ *    (W-1) x H; vy is W x (H-1).
+ *  - Host pointers ("const float *" arguments of the non-_device calls) are
+ *    plain host memory; the call copies through the handle's own stream and
+ *    returns after the copy is complete.
+ *  - Every function returns UBG_OK (0) or a negative UBG_E* code; the message
+ *    of the last error on the calling thread is ubg_last_error().  No C++
+ *    exception crosses this boundary.  The reference has no error path (void
+ *    functions, asserts compiled out by -DNDEBUG).
+ *  - Flags must be exactly 0.0 (solid) or 1.0 (fluid), which is what the
+ *    reference's terrain produces (terrain.cpp:3-11); they are stored on the
+ *    device as one byte per cell.  Other values are rejected (UBG_EINVAL).
+ *  - One CUDA stream per handle; distinct handles may be used from different
+ *    threads.  A handle must not be used by two threads at once.
+ *  - No CPU fallback: without a usable CUDA device every call that needs the
+ *    GPU returns UBG_ECUDA.
+ */
+#ifndef UBOOTGL_GB300_H
+#define UBOOTGL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UBG_OK 0
+#define UBG_EINVAL -1  /* bad argument (size, flag value, field id, ...) */
+#define UBG_ECUDA -2   /* CUDA runtime error (message in ubg_last_error) */
+#define UBG_ENOMEM -3  /* device or host allocation failed / over budget */
+#define UBG_ESTATE -4  /* call not valid in the current state */
+#define UBG_ETIMEOUT -5 /* a bounded device-side wait ran out */
+#define UBG_EBUSY -6   /* admission refused (server at capacity) */
+
+/* Boundary types, Simulation::BC (simulation.hpp:69). */
+enum ubg_bc { UBG_BC_INFLOW = 0, UBG_BC_OUTFLOW = 1, UBG_BC_OUTFLOW_ZERO_PRESSURE = 2, UBG_BC_NOSLIP = 3 };
+
+/* Fields of Simulation (simulation.hpp:128-134).  VX/VY are the front
+ * buffers (vx.f(), vy.f()); VX_BACK/VY_BACK the back buffers (vx.b()).
+ * VX_CURRENT/VY_CURRENT are the display copies that step() leaves
+ * (saveCurrentVelocityFields, simulation.cpp:16-19); they read the front
+ * buffer as of the end of the last step.  FLAG is read/written as float. */
+enum ubg_field {
+  UBG_VX = 0,
+  UBG_VY = 1,
+  UBG_VX_BACK = 2,
+  UBG_VY_BACK = 3,
+  UBG_P = 4,
+  UBG_F = 5,
+  UBG_FLAG = 6,
+  UBG_VX_ACCUM = 7,
+  UBG_VY_ACCUM = 8,
+  UBG_VX_CURRENT = 9,
+  UBG_VY_CURRENT = 10
+};
+
+/* Pressure-solver policy (extension; the reference always runs exactly two
+ * V-cycles, simulation.cpp:189-190, and never looks at the residual). */
+enum ubg_solver_mode {
+  UBG_SOLVE_FIXED = 0,     /* `vcycles` V-cycles (2 = the reference) */
+  UBG_SOLVE_TOLERANCE = 1  /* V-cycles until ||r||/||r0|| <= tol or max_vcycles */
+};
+
+/* Precision of the multigrid corrections (extension).  FP32 is the
+ * reference's arithmetic.  MIXED_* run an FP32 defect-correction loop whose
+ * inner V-cycle stores and smooths the error equation in FP16 / BF16, with
+ * FP64 global norms and an FP64 coarsest-level solve. */
+enum ubg_precision { UBG_FP32 = 0, UBG_MIXED_FP16 = 1, UBG_MIXED_BF16 = 2 };
+
+typedef struct ubg_options {
+  int solver_mode;    /* ubg_solver_mode, default UBG_SOLVE_FIXED */
+  int vcycles;        /* FIXED mode: V-cycles per projection, default 2 */
+  float tol;          /* TOLERANCE mode: relative residual target, default 1e-6 */
+  int max_vcycles;    /* TOLERANCE mode: cap, default 100 */
+  int precision;      /* ubg_precision, default UBG_FP32 */
+  int use_graph;      /* capture the step into a CUDA graph, default 1 */
+} ubg_options;
+
+typedef struct ubg_sim ubg_sim;
+typedef struct ubg_mg ubg_mg;
+
+/* Last error message of the calling thread ("" if none). */
+const char *ubg_last_error(void);
+
+/* Library / device information: writes a short JSON object. */
+int ubg_device_info(char *buf, size_t len);
+
+/* Page-locked host memory for fast ubg_upload / ubg_download (extension; the
+ * reference keeps its fields in std::vector). */
+int ubg_host_alloc(size_t bytes, void **ptr);
+int ubg_host_free(void *ptr);
+
+/* ---------------------------------------------------------- Simulation */
+
+/* Simulation(const Single2DGrid &flag, float pwidth, float mu),
+ * simulation.hpp:32-67: allocates all fields on the device, sets the
+ * reference's boundary types (W inflow, E outflow with zero pressure, N/S
+ * no-slip), vy(x,0) = 0 and vx(0,y) = 1 in both buffers, h = pwidth/(W-1),
+ * and builds the multigrid hierarchy from `flag` (MG(flag)).  W, H >= 8. */
+int ubg_create(const float *flag, int width, int height, float pwidth, float mu, ubg_sim **out);
+int ubg_destroy(ubg_sim *sim);
+
+/* Solver options (see ubg_options); applies from the next step. */
+int ubg_default_options(ubg_options *opt);
+int ubg_set_options(ubg_sim *sim, const ubg_options *opt);
+
+/* bcWest/bcEast/bcNorth/bcSouth members (simulation.hpp:124). */
+int ubg_set_bcs(ubg_sim *sim, int west, int east, int north, int south);
+
+/* Simulation::step(float timestep), simulation.cpp:356-374:
+ * applyAccumulatedVelocity, diffuse, advect, setVBCs, project, setVBCs,
+ * saveCurrentVelocityFields.  Enqueued on the handle's stream; returns when
+ * enqueued (ubg_sync waits). */
+int ubg_step(ubg_sim *sim, float dt);
+
+/* The same step with dt = cfl * h / max|u| computed on the device from the
+ * current fields (extension: the reference takes dt from its caller,
+ * sim_loop.cpp:28).  The dt used is readable with ubg_last_dt after a sync. */
+int ubg_step_cfl(ubg_sim *sim, float cfl);
+int ubg_last_dt(ubg_sim *sim, float *dt);
+
+/* Individual stages of the step, for callers that drive them one by one and
+ * for stage-wise parity tests.  `dt` sets the member Simulation::dt first. */
+int ubg_apply_accumulated_velocity(ubg_sim *sim); /* simulation.cpp:376-396 */
+int ubg_diffuse(ubg_sim *sim, float dt);          /* simulation.cpp:104-162 */
+int ubg_advect(ubg_sim *sim, float dt);           /* simulation.cpp:241-354 */
+int ubg_set_vbcs(ubg_sim *sim);                   /* simulation.cpp:80-102 */
+int ubg_set_pbc(ubg_sim *sim);                    /* simulation.cpp:36-45 */
+int ubg_project(ubg_sim *sim, float dt);          /* simulation.cpp:164-208 */
+
+/* sinks.push_back(glm::vec3(x, y, strength)) (explosion.cpp:33); consumed
+ * by project() (simulation.cpp:173-187). */
+int ubg_add_sink(ubg_sim *sim, float x, float y, float strength);
+
+/* Host <-> device copies of one field (see ubg_field).  Uploading UBG_FLAG
+ * is memcpy(sim.flag.data(), ...) followed by mg.updateFields(sim.flag)
+ * (ubootgl_app.cpp:111-112): the coarse flags are rebuilt on the device. */
+int ubg_upload(ubg_sim *sim, int field, const float *src);
+int ubg_download(ubg_sim *sim, int field, float *dst);
+
+/* Multigrid of the simulation: number of levels, size and (float) flag of
+ * one level (MG::flagcs, pressure_solver.hpp:72). */
+int ubg_mg_levels(ubg_sim *sim, int *levels);
+int ubg_mg_level_flag(ubg_sim *sim, int level, int *w, int *h, float *dst);
+
+/* Runs the simulation's mg.solve(p, f, flag, h, zeroGradientBC) once
+ * (pressure_solver.hpp:59-62) on the device-resident p and f. */
+int ubg_mg_solve_sim(ubg_sim *sim, int zero_gradient_bc);
+
+/* Device views for zero-copy composition with other CUDA code: pointer,
+ * row pitch in elements, width, height.  Valid until the next step (the
+ * velocity buffers rotate). FLAG is uint8 (one byte per cell). */
+int ubg_field_device(ubg_sim *sim, int field, void **ptr, int *pitch, int *w, int *h);
+/* The handle's cudaStream_t. */
+int ubg_stream(ubg_sim *sim, void **stream);
+int ubg_sync(ubg_sim *sim);
+
+/* Per-kernel timing (extension, for the benchmark).  While enabled, steps
+ * run as direct launches (no graph) with a CUDA event pair around every
+ * kernel; ubg_profile_read gives the mean level-0 smoother launch time, the
+ * mean profiled step time and the launch count of the last step;
+ * ubg_profile_class gives the accumulated time and launch count of one
+ * kernel class (0 <= kc < 17, name returned). */
+int ubg_profile_enable(ubg_sim *sim, int on);
+int ubg_profile_read(ubg_sim *sim, double *smoother_ms, int *smoother_launches,
+                     double *step_ms, int *kernel_launches);
+int ubg_profile_class(ubg_sim *sim, int kc, const char **name, double *total_ms, int *count);
+int ubg_profile_reset(ubg_sim *sim);
+
+/* --------------------------------------------------------------- class MG */
+
+/* MG(int width, int height) (pressure_solver.hpp:16-31), with every coarse
+ * flag 1.0; flag != NULL gives MG(Single2DGrid &flag) (pressure_solver.hpp:32),
+ * which also runs updateFields(flag). */
+int ubg_mg_create(int width, int height, const float *flag, ubg_mg **out);
+int ubg_mg_destroy(ubg_mg *mg);
+/* MG::updateFields(flag), pressure_solver.hpp:34-57. */
+int ubg_mg_update_fields(ubg_mg *mg, const float *flag);
+/* MG::solve(p, f, flag, h, zeroGradientBC), pressure_solver.hpp:59-62, on
+ * host arrays of width x height; p is updated in place. */
+int ubg_mg_solve(ubg_mg *mg, float *p, const float *f, const float *flag, float h,
+                 int zero_gradient_bc);
+/* Same, on device arrays (row pitch in elements; flag as uint8), enqueued on
+ * `stream` (a cudaStream_t, NULL = the handle's stream). */
+int ubg_mg_solve_device(ubg_mg *mg, float *p, int p_pitch, const float *f, int f_pitch,
+                        const uint8_t *flag, int flag_pitch, float h, int zero_gradient_bc,
+                        void *stream);
+
+/* Free functions of pressure_solver.hpp:3-11 on host arrays:
+ * rbgs(p, f, flag, h, alpha) (one red-black sweep, pressure_solver.cpp:35-89)
+ * and calculateResidualField(p, f, flag, r, h) (pressure_solver.cpp:91-116;
+ * the L2 norm is accumulated in double). */
+int ubg_rbgs(float *p, const float *f, const float *flag, int width, int height, float h,
+             float alpha);
+int ubg_residual(const float *p, const float *f, const float *flag, float *r, int width,
+                 int height, float h, double *l2norm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UBOOTGL_GB300_H */

@@ -1,0 +1,924 @@
+// C ABI of ubootgl_gb300 (include/ubootgl_gb300.h): simulation handles,
+// host <-> device transfers, the step sequence of Simulation::step
+// (simulation.cpp:356-374), the standalone MG class and the free solver
+// functions.  All device work of a handle goes to its own stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ubg_internal.cuh"
+
+using namespace ubg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    g_err.clear();
+    return f();
+  } catch (const ArgError &e) {
+    return fail(UBG_EINVAL, e.what());
+  } catch (const CudaError &e) {
+    return fail(UBG_ECUDA, e.what());
+  } catch (const std::bad_alloc &) {
+    return fail(UBG_ENOMEM, "allocation failed");
+  } catch (const std::exception &e) {
+    return fail(UBG_ESTATE, e.what());
+  }
+}
+
+constexpr int kRing = 64;
+constexpr int kMaxSinks = 256;
+
+// Flags cross the ABI as float 0.0 / 1.0 and live on the device as bytes.
+void flag_to_u8(const float *flag, int W, int H, std::vector<uint8_t> &out, int pitch) {
+  out.assign((size_t)pitch * H, 0);
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      float v = flag[(size_t)y * W + x];
+      if (v == 0.0f)
+        out[(size_t)y * pitch + x] = 0;
+      else if (v == 1.0f)
+        out[(size_t)y * pitch + x] = 1;
+      else
+        throw ArgError("flag values must be exactly 0.0 or 1.0 (cell " + std::to_string(x) + "," +
+                       std::to_string(y) + ")");
+    }
+}
+
+StepScalars make_scalars(float dt, float mu, float pwidth, int W, float h) {
+  // simulation.cpp:105, 165, 242, 276, 286
+  StepScalars s;
+  s.dt = dt;
+  s.a = dt * mu * ((float)W - 1.0f) / pwidth;
+  s.den = 1.0f + 4.0f * s.a;
+  s.ih = 1.0f / h;
+  s.chalf = 0.5f * dt * s.ih;
+  s.cfull = dt * s.ih;
+  return s;
+}
+
+struct HostSink {
+  float x, y, z;
+};
+
+}  // namespace
+
+struct ubg_sim {
+  int W = 0, H = 0, P = 0;
+  float pwidth = 1.0f, mu = 0.0f, h = 0.0f;
+  Bcs bc{UBG_BC_INFLOW, UBG_BC_OUTFLOW_ZERO_PRESSURE, UBG_BC_NOSLIP, UBG_BC_NOSLIP};
+  ubg_options opt{};
+  cudaStream_t st = nullptr;
+  void *arena = nullptr;
+  VelBufs v{};
+  int fx = 0, fy = 0;
+  float *ax = nullptr, *ay = nullptr;
+  MgHier mg;
+  StepScalars *d_sc = nullptr;
+  unsigned int *d_umax = nullptr;
+  SinkCell *d_sinks = nullptr;
+  // pinned host staging
+  StepScalars *h_ring = nullptr;
+  SinkCell *h_sinks = nullptr;
+  double *h_norm = nullptr;
+  cudaEvent_t ring_ev[kRing] = {};
+  bool ring_used[kRing] = {};
+  int ring_i = 0;
+  std::vector<HostSink> sinks;
+  std::vector<float> flag_host;
+  bool accum_dirty = false;
+  float last_dt = 0.0f;
+  int last_vcycles = 0;
+  // CUDA graph of the fixed-cycle step body
+  cudaGraphExec_t graph = nullptr;
+  int graph_key = -1;
+  // profiling
+  bool prof = false;
+  Profiler profiler;
+  cudaEvent_t ev_step[2] = {nullptr, nullptr};
+  long launches_last = 0;
+  double step_ms_total = 0.0;
+  long steps_profiled = 0;
+
+  ~ubg_sim() {
+    if (st) cudaStreamSynchronize(st);
+    if (graph) cudaGraphExecDestroy(graph);
+    for (auto &e : ring_ev)
+      if (e) cudaEventDestroy(e);
+    for (auto &e : ev_step)
+      if (e) cudaEventDestroy(e);
+    if (h_ring) cudaFreeHost(h_ring);
+    if (h_sinks) cudaFreeHost(h_sinks);
+    if (h_norm) cudaFreeHost(h_norm);
+    mg_free(mg);
+    if (arena) cudaFree(arena);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  float *p() { return mg.lv[0].e[mg.cur0]; }
+  float *f() { return mg.lv[0].rhs; }
+  uint8_t *flag() { return mg.lv[0].flag; }
+
+  // Stages the dt-dependent scalars for the next kernels of this stream.
+  void push_scalars(float dt) {
+    int slot = ring_i;
+    ring_i = (ring_i + 1) % kRing;
+    if (ring_used[slot]) UBG_CUDA(cudaEventSynchronize(ring_ev[slot]));
+    h_ring[slot] = make_scalars(dt, mu, pwidth, W, h);
+    UBG_CUDA(cudaMemcpyAsync(d_sc, &h_ring[slot], sizeof(StepScalars), cudaMemcpyHostToDevice, st));
+    UBG_CUDA(cudaEventRecord(ring_ev[slot], st));
+    ring_used[slot] = true;
+    last_dt = dt;
+  }
+
+  void set_vbcs() { launch_vbc(v, fx, fy, bc, true, true, st); }
+
+  void apply_accum() {
+    launch_accum(v, fx, fy, ax, ay, st);
+    accum_dirty = false;
+  }
+
+  // diffuse(), simulation.cpp:104-162.  The vx and vy sweeps are independent
+  // (setVBCs treats the components separately), so each sweep launch does
+  // both; the vy boundary is refreshed first because the reference's vy
+  // sweeps run after a setVBCs.
+  void diffuse() {
+    launch_vbc(v, fx, fy, bc, false, true, st);
+    for (int i = 0; i < 2; i++) {
+      launch_diffuse_sweep(v, fx, fy, flag(), d_sc, 3, st);
+      fx ^= 1;
+      fy ^= 1;
+      set_vbcs();
+    }
+  }
+
+  void advect() {
+    launch_advect(v, fx, fy, flag(), d_sc, st);
+    fx ^= 1;
+    fy ^= 1;
+  }
+
+  // The sinks of project() (simulation.cpp:173-187), resolved on the host.
+  int stage_sinks(float dt) {
+    int n = 0;
+    std::vector<HostSink> keep;
+    for (auto &s : sinks) {
+      float gx = s.x / h + 0.5f, gy = s.y / h + 0.5f;
+      if (!(gx <= 3 || gx > (float)(W - 3) || gy <= 3 || gy > (float)(H - 3))) {
+        for (int dy = -1; dy <= 1; dy++)
+          for (int dx = -1; dx <= 1; dx++) {
+            if (n >= kMaxSinks * 9) break;
+            h_sinks[n++] = SinkCell{(int)(gx + (float)dx), (int)(gy + (float)dy), s.z};
+          }
+        s.z = (float)((double)s.z * std::pow(0.000001, (double)(dt * 50.0f)));
+      }
+    }
+    for (auto &s : sinks)
+      if (!(s.z < 0.05f)) keep.push_back(s);
+    sinks.swap(keep);
+    if (n) UBG_CUDA(cudaMemcpyAsync(d_sinks, h_sinks, sizeof(SinkCell) * n, cudaMemcpyHostToDevice, st));
+    return n;
+  }
+
+  void solve_pressure() {
+    if (opt.solver_mode == UBG_SOLVE_TOLERANCE) {
+      solve_tolerance();
+      return;
+    }
+    for (int c = 0; c < opt.vcycles; c++) mg_solve(mg, true, st);
+    last_vcycles = opt.vcycles;
+  }
+
+  // Extension: V-cycles until ||r|| <= tol * ||f|| (FP64 norms).
+  void solve_tolerance() {
+    MgLevel &L0 = mg.lv[0];
+    int c = 0;
+    double fnorm2 = 0.0;
+    level_residual_of_rhs(L0, &fnorm2);
+    double target2 = (double)opt.tol * (double)opt.tol * fnorm2;
+    for (c = 0; c < opt.max_vcycles; c++) {
+      mg_solve(mg, true, st);
+      UBG_CUDA(cudaMemsetAsync(mg.norm, 0, sizeof(double), st));
+      level_residual(L0, mg.cur0, nullptr, mg.norm, st);
+      UBG_CUDA(cudaMemcpyAsync(h_norm, mg.norm, sizeof(double), cudaMemcpyDeviceToHost, st));
+      UBG_CUDA(cudaStreamSynchronize(st));
+      if (*h_norm <= target2) {
+        c++;
+        break;
+      }
+    }
+    last_vcycles = c;
+  }
+
+  void level_residual_of_rhs(MgLevel &L0, double *out) {
+    // ||f * flag|| is the residual of p = 0: run the residual kernel on the
+    // idle ping-pong buffer after zeroing it.
+    float *zero = L0.e[1 - mg.cur0];
+    UBG_CUDA(cudaMemsetAsync(zero, 0, sizeof(float) * (size_t)L0.pitch * L0.h, st));
+    UBG_CUDA(cudaMemsetAsync(mg.norm, 0, sizeof(double), st));
+    level_residual(L0, 1 - mg.cur0, nullptr, mg.norm, st);
+    UBG_CUDA(cudaMemcpyAsync(h_norm, mg.norm, sizeof(double), cudaMemcpyDeviceToHost, st));
+    UBG_CUDA(cudaStreamSynchronize(st));
+    *out = *h_norm;
+  }
+
+  // project(), simulation.cpp:164-208 (without the trailing setVBCs of step).
+  void project(int nsink_cells) {
+    launch_divergence(v, fx, fy, f(), d_sc, st);
+    launch_sinks(f(), P, d_sinks, nsink_cells, st);
+    solve_pressure();
+    launch_pbc(p(), P, W, H, bc, st);
+    launch_gradient(v, fx, fy, p(), flag(), d_sc, st);
+  }
+
+  // Everything of step() after the scalars are staged and the accumulated
+  // velocity is applied; captured into a graph in fixed-cycle mode.
+  void step_body(int nsink_cells) {
+    diffuse();
+    advect();
+    set_vbcs();
+    project(nsink_cells);
+    set_vbcs();
+  }
+
+  void step(float dt, bool device_dt, float cfl) {
+    long l0 = g_stats.launches;
+    struct ProfInstall {
+      bool on;
+      ProfInstall(bool on_, Profiler *p) : on(on_) {
+        if (on) g_prof = p;
+      }
+      ~ProfInstall() {
+        if (on) g_prof = nullptr;
+      }
+    } pi(prof, &profiler);
+    if (prof) UBG_CUDA(cudaEventRecord(ev_step[0], st));
+    if (accum_dirty) apply_accum();
+    int nsc = 0;
+    if (device_dt) {
+      launch_cfl(v, fx, fy, cfl, h, mu, pwidth, d_umax, d_sc, st);
+    } else {
+      push_scalars(dt);
+      nsc = sinks.empty() ? 0 : stage_sinks(dt);
+    }
+    bool graphable = opt.use_graph && opt.solver_mode == UBG_SOLVE_FIXED && nsc == 0 && !prof;
+    if (graphable) {
+      // The body only depends on (fx, fy, cur0) parity and the cycle count.
+      int key = (fx << 2) | (fy << 1) | mg.cur0 | (opt.vcycles << 3);
+      if (!graph || graph_key != key) capture(key);
+      UBG_CUDA(cudaGraphLaunch(graph, st));
+      // replay the index bookkeeping of the captured body
+      advance_indices();
+      g_stats.launches += graph_launches;
+    } else {
+      step_body(nsc);
+    }
+    if (prof) {
+      UBG_CUDA(cudaEventRecord(ev_step[1], st));
+      // per-step collection keeps the event pool small
+      UBG_CUDA(cudaStreamSynchronize(st));
+      float ms = 0.0f;
+      UBG_CUDA(cudaEventElapsedTime(&ms, ev_step[0], ev_step[1]));
+      step_ms_total += ms;
+      steps_profiled++;
+      profiler.collect();
+    }
+    launches_last = g_stats.launches - l0;
+  }
+
+  long graph_launches = 0;
+  int after_fx = 0, after_fy = 0, after_cur0 = 0;
+
+  void capture(int key) {
+    if (graph) {
+      cudaGraphExecDestroy(graph);
+      graph = nullptr;
+    }
+    int fx0 = fx, fy0 = fy, c0 = mg.cur0;
+    long l0 = g_stats.launches;
+    cudaGraph_t g = nullptr;
+    UBG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      step_body(0);
+    } catch (...) {
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    UBG_CUDA(cudaStreamEndCapture(st, &g));
+    UBG_CUDA(cudaGraphInstantiate(&graph, g, 0));
+    cudaGraphDestroy(g);
+    graph_launches = g_stats.launches - l0;
+    g_stats.launches = l0;
+    after_fx = fx;
+    after_fy = fy;
+    after_cur0 = mg.cur0;
+    fx = fx0;
+    fy = fy0;
+    mg.cur0 = c0;
+    graph_key = key;
+  }
+
+  void advance_indices() {
+    fx = after_fx;
+    fy = after_fy;
+    mg.cur0 = after_cur0;
+  }
+
+  void sync() { UBG_CUDA(cudaStreamSynchronize(st)); }
+};
+
+struct ubg_mg {
+  MgHier mg;
+  cudaStream_t st = nullptr;
+  int W = 0, H = 0;
+  ~ubg_mg() {
+    if (st) cudaStreamSynchronize(st);
+    mg_free(mg);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+namespace {
+
+struct FieldView {
+  float *dev;
+  int w, h;
+};
+
+FieldView field_view(ubg_sim *s, int field) {
+  int W = s->W, H = s->H;
+  switch (field) {
+    case UBG_VX: case UBG_VX_CURRENT: return {s->v.vx[s->fx], W - 1, H};
+    case UBG_VY: case UBG_VY_CURRENT: return {s->v.vy[s->fy], W, H - 1};
+    case UBG_VX_BACK: return {s->v.vx[1 - s->fx], W - 1, H};
+    case UBG_VY_BACK: return {s->v.vy[1 - s->fy], W, H - 1};
+    case UBG_P: return {s->p(), W, H};
+    case UBG_F: return {s->f(), W, H};
+    case UBG_VX_ACCUM: return {s->ax, W - 1, H};
+    case UBG_VY_ACCUM: return {s->ay, W, H - 1};
+  }
+  throw ArgError("unknown field id " + std::to_string(field));
+}
+
+void upload_flag_u8(MgLevel &L0, const float *flag, int W, int H, cudaStream_t st) {
+  std::vector<uint8_t> u8;
+  flag_to_u8(flag, W, H, u8, L0.pitch);
+  UBG_CUDA(cudaMemcpyAsync(L0.flag, u8.data(), u8.size(), cudaMemcpyHostToDevice, st));
+  UBG_CUDA(cudaStreamSynchronize(st));
+}
+
+void check_device() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    throw CudaError("no CUDA device available (this library has no CPU path)");
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ubg_last_error(void) { return g_err.c_str(); }
+
+int ubg_device_info(char *buf, size_t len) {
+  return guarded([&] {
+    check_device();
+    int dev = 0;
+    UBG_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    UBG_CUDA(cudaGetDeviceProperties(&p, dev));
+    snprintf(buf, len, "{\"name\": \"%s\", \"sm\": \"%d.%d\", \"sms\": %d, \"mem_gb\": %.1f}", p.name,
+             p.major, p.minor, p.multiProcessorCount, p.totalGlobalMem / 1e9);
+    return UBG_OK;
+  });
+}
+
+int ubg_host_alloc(size_t bytes, void **ptr) {
+  return guarded([&] {
+    if (!ptr) throw ArgError("null argument");
+    check_device();
+    UBG_CUDA(cudaMallocHost(ptr, bytes));
+    return UBG_OK;
+  });
+}
+
+int ubg_host_free(void *ptr) {
+  return guarded([&] {
+    if (ptr) UBG_CUDA(cudaFreeHost(ptr));
+    return UBG_OK;
+  });
+}
+
+int ubg_default_options(ubg_options *o) {
+  if (!o) return fail(UBG_EINVAL, "null options");
+  o->solver_mode = UBG_SOLVE_FIXED;
+  o->vcycles = 2;
+  o->tol = 1e-6f;
+  o->max_vcycles = 100;
+  o->precision = UBG_FP32;
+  o->use_graph = 1;
+  return UBG_OK;
+}
+
+int ubg_create(const float *flag, int width, int height, float pwidth, float mu, ubg_sim **out) {
+  return guarded([&] {
+    if (!flag || !out) throw ArgError("null argument");
+    if (width < 8 || height < 8) throw ArgError("width and height must be >= 8");
+    if ((long long)width * height > (1LL << 31)) throw ArgError("grid too large");
+    check_device();
+    std::unique_ptr<ubg_sim> s(new ubg_sim());
+    s->W = width;
+    s->H = height;
+    s->P = round_up(width, 32);
+    s->pwidth = pwidth;
+    s->mu = mu;
+    s->h = pwidth / ((float)width - 1.0f);  // simulation.hpp:63
+    ubg_default_options(&s->opt);
+    UBG_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    size_t n = (size_t)s->P * height;
+    size_t fb = (n * 4 + 255) / 256 * 256;
+    size_t extra = 256 * 3 + (size_t)kMaxSinks * 9 * sizeof(SinkCell);
+    size_t total = 6 * fb + extra;
+    if (cudaMalloc(&s->arena, total) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    UBG_CUDA(cudaMemsetAsync(s->arena, 0, total, s->st));
+    char *p = (char *)s->arena;
+    s->v.vx[0] = (float *)p; p += fb;
+    s->v.vx[1] = (float *)p; p += fb;
+    s->v.vy[0] = (float *)p; p += fb;
+    s->v.vy[1] = (float *)p; p += fb;
+    s->ax = (float *)p; p += fb;
+    s->ay = (float *)p; p += fb;
+    s->d_sc = (StepScalars *)p; p += 256;
+    s->d_umax = (unsigned int *)p; p += 256;
+    p += 256;
+    s->d_sinks = (SinkCell *)p;
+    s->v.pitch = s->P;
+    s->v.W = width;
+    s->v.H = height;
+    mg_alloc(s->mg, width, height, s->h);
+    UBG_CUDA(cudaMallocHost(&s->h_ring, sizeof(StepScalars) * kRing));
+    UBG_CUDA(cudaMallocHost(&s->h_sinks, sizeof(SinkCell) * kMaxSinks * 9));
+    UBG_CUDA(cudaMallocHost(&s->h_norm, sizeof(double)));
+    for (auto &e : s->ring_ev) UBG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &e : s->ev_step) UBG_CUDA(cudaEventCreate(&e));
+    // flag + multigrid hierarchy (MG(flag), simulation.hpp:62)
+    s->flag_host.assign(flag, flag + (size_t)width * height);
+    upload_flag_u8(s->mg.lv[0], flag, width, height, s->st);
+    mg_update_fields(s->mg, s->st);
+    // vy(x, 0) = 0 and vx(0, y) = 1 in both buffers (simulation.hpp:55-60)
+    std::vector<float> col((size_t)height, 1.0f);
+    for (int b = 0; b < 2; b++)
+      UBG_CUDA(cudaMemcpy2DAsync(s->v.vx[b], (size_t)s->P * 4, col.data(), 4, 4, height,
+                                 cudaMemcpyHostToDevice, s->st));
+    UBG_CUDA(cudaStreamSynchronize(s->st));
+    *out = s.release();
+    return UBG_OK;
+  });
+}
+
+int ubg_destroy(ubg_sim *sim) {
+  return guarded([&] {
+    delete sim;
+    return UBG_OK;
+  });
+}
+
+int ubg_set_options(ubg_sim *s, const ubg_options *o) {
+  return guarded([&] {
+    if (!s || !o) throw ArgError("null argument");
+    if (o->solver_mode != UBG_SOLVE_FIXED && o->solver_mode != UBG_SOLVE_TOLERANCE)
+      throw ArgError("solver_mode");
+    if (o->vcycles < 0 || o->vcycles > 1000) throw ArgError("vcycles out of range");
+    if (o->max_vcycles < 1 || o->max_vcycles > 100000) throw ArgError("max_vcycles out of range");
+    if (o->precision != UBG_FP32) throw ArgError("precision mode not available on a simulation handle");
+    s->opt = *o;
+    s->graph_key = -1;
+    return UBG_OK;
+  });
+}
+
+int ubg_set_bcs(ubg_sim *s, int west, int east, int north, int south) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    for (int b : {west, east, north, south})
+      if (b < 0 || b > 3) throw ArgError("boundary type");
+    s->bc = Bcs{west, east, north, south};
+    s->graph_key = -1;  // boundary types are baked into the captured step
+    return UBG_OK;
+  });
+}
+
+int ubg_step(ubg_sim *s, float dt) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->step(dt, false, 0.0f);
+    return UBG_OK;
+  });
+}
+
+int ubg_step_cfl(ubg_sim *s, float cfl) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    if (!s->sinks.empty()) throw ArgError("sinks need a host dt (use ubg_step)");
+    s->step(0.0f, true, cfl);
+    return UBG_OK;
+  });
+}
+
+int ubg_last_dt(ubg_sim *s, float *dt) {
+  return guarded([&] {
+    if (!s || !dt) throw ArgError("null argument");
+    StepScalars sc;
+    UBG_CUDA(cudaMemcpyAsync(&sc, s->d_sc, sizeof(sc), cudaMemcpyDeviceToHost, s->st));
+    UBG_CUDA(cudaStreamSynchronize(s->st));
+    *dt = sc.dt;
+    return UBG_OK;
+  });
+}
+
+int ubg_apply_accumulated_velocity(ubg_sim *s) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->apply_accum();
+    return UBG_OK;
+  });
+}
+
+int ubg_diffuse(ubg_sim *s, float dt) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->push_scalars(dt);
+    s->diffuse();
+    return UBG_OK;
+  });
+}
+
+int ubg_advect(ubg_sim *s, float dt) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->push_scalars(dt);
+    s->advect();
+    return UBG_OK;
+  });
+}
+
+int ubg_set_vbcs(ubg_sim *s) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->set_vbcs();
+    return UBG_OK;
+  });
+}
+
+int ubg_set_pbc(ubg_sim *s) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    launch_pbc(s->p(), s->P, s->W, s->H, s->bc, s->st);
+    return UBG_OK;
+  });
+}
+
+int ubg_project(ubg_sim *s, float dt) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->push_scalars(dt);
+    int n = s->sinks.empty() ? 0 : s->stage_sinks(dt);
+    s->project(n);
+    return UBG_OK;
+  });
+}
+
+int ubg_add_sink(ubg_sim *s, float x, float y, float strength) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    if ((int)s->sinks.size() >= kMaxSinks) throw ArgError("too many sinks");
+    s->sinks.push_back(HostSink{x, y, strength});
+    return UBG_OK;
+  });
+}
+
+int ubg_upload(ubg_sim *s, int field, const float *src) {
+  return guarded([&] {
+    if (!s || !src) throw ArgError("null argument");
+    if (field == UBG_FLAG) {
+      upload_flag_u8(s->mg.lv[0], src, s->W, s->H, s->st);
+      s->flag_host.assign(src, src + (size_t)s->W * s->H);
+      mg_update_fields(s->mg, s->st);
+      s->sync();
+      return UBG_OK;
+    }
+    if (field == UBG_VX_CURRENT || field == UBG_VY_CURRENT) throw ArgError("current fields are read-only");
+    FieldView fv = field_view(s, field);
+    UBG_CUDA(cudaMemcpy2DAsync(fv.dev, (size_t)s->P * 4, src, (size_t)fv.w * 4, (size_t)fv.w * 4, fv.h,
+                               cudaMemcpyHostToDevice, s->st));
+    if (field == UBG_VX_ACCUM || field == UBG_VY_ACCUM) s->accum_dirty = true;
+    s->sync();
+    return UBG_OK;
+  });
+}
+
+int ubg_download(ubg_sim *s, int field, float *dst) {
+  return guarded([&] {
+    if (!s || !dst) throw ArgError("null argument");
+    if (field == UBG_FLAG) {
+      s->sync();
+      std::memcpy(dst, s->flag_host.data(), sizeof(float) * s->flag_host.size());
+      return UBG_OK;
+    }
+    FieldView fv = field_view(s, field);
+    UBG_CUDA(cudaMemcpy2DAsync(dst, (size_t)fv.w * 4, fv.dev, (size_t)s->P * 4, (size_t)fv.w * 4, fv.h,
+                               cudaMemcpyDeviceToHost, s->st));
+    s->sync();
+    return UBG_OK;
+  });
+}
+
+int ubg_mg_levels(ubg_sim *s, int *levels) {
+  return guarded([&] {
+    if (!s || !levels) throw ArgError("null argument");
+    *levels = s->mg.levels;
+    return UBG_OK;
+  });
+}
+
+int ubg_mg_level_flag(ubg_sim *s, int level, int *w, int *h, float *dst) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    if (level < 0 || level >= s->mg.levels) throw ArgError("level out of range");
+    MgLevel &L = s->mg.lv[level];
+    if (w) *w = L.w;
+    if (h) *h = L.h;
+    if (!dst) return UBG_OK;
+    std::vector<uint8_t> u8((size_t)L.pitch * L.h);
+    UBG_CUDA(cudaMemcpyAsync(u8.data(), L.flag, u8.size(), cudaMemcpyDeviceToHost, s->st));
+    s->sync();
+    for (int y = 0; y < L.h; y++)
+      for (int x = 0; x < L.w; x++) dst[(size_t)y * L.w + x] = (float)u8[(size_t)y * L.pitch + x];
+    return UBG_OK;
+  });
+}
+
+int ubg_mg_solve_sim(ubg_sim *s, int zgbc) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    mg_solve(s->mg, zgbc != 0, s->st);
+    return UBG_OK;
+  });
+}
+
+int ubg_field_device(ubg_sim *s, int field, void **ptr, int *pitch, int *w, int *h) {
+  return guarded([&] {
+    if (!s || !ptr) throw ArgError("null argument");
+    if (field == UBG_FLAG) {
+      *ptr = s->flag();
+      if (pitch) *pitch = s->P;
+      if (w) *w = s->W;
+      if (h) *h = s->H;
+      return UBG_OK;
+    }
+    FieldView fv = field_view(s, field);
+    *ptr = fv.dev;
+    if (pitch) *pitch = s->P;
+    if (w) *w = fv.w;
+    if (h) *h = fv.h;
+    return UBG_OK;
+  });
+}
+
+int ubg_stream(ubg_sim *s, void **stream) {
+  if (!s || !stream) return fail(UBG_EINVAL, "null argument");
+  *stream = (void *)s->st;
+  return UBG_OK;
+}
+
+int ubg_sync(ubg_sim *s) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->sync();
+    return UBG_OK;
+  });
+}
+
+int ubg_profile_enable(ubg_sim *s, int on) {
+  if (!s) return fail(UBG_EINVAL, "null handle");
+  s->prof = on != 0;
+  return UBG_OK;
+}
+
+int ubg_profile_read(ubg_sim *s, double *smoother_ms, int *smoother_launches, double *step_ms,
+                     int *kernel_launches) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->sync();
+    long n = s->profiler.count[KC_SMOOTH_L0];
+    if (smoother_ms) *smoother_ms = n ? s->profiler.total_ms[KC_SMOOTH_L0] / n : 0.0;
+    if (smoother_launches) *smoother_launches = (int)n;
+    if (step_ms) *step_ms = s->steps_profiled ? s->step_ms_total / s->steps_profiled : 0.0;
+    if (kernel_launches) *kernel_launches = (int)s->launches_last;
+    return UBG_OK;
+  });
+}
+
+int ubg_profile_class(ubg_sim *s, int kc, const char **name, double *total_ms, int *count) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    if (kc < 0 || kc >= KC_COUNT) throw ArgError("kernel class out of range");
+    s->sync();
+    if (name) *name = kernel_class_name(kc);
+    if (total_ms) *total_ms = s->profiler.total_ms[kc];
+    if (count) *count = (int)s->profiler.count[kc];
+    return UBG_OK;
+  });
+}
+
+int ubg_profile_reset(ubg_sim *s) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->sync();
+    for (int k = 0; k < KC_COUNT; k++) {
+      s->profiler.total_ms[k] = 0.0;
+      s->profiler.count[k] = 0;
+    }
+    s->step_ms_total = 0.0;
+    s->steps_profiled = 0;
+    return UBG_OK;
+  });
+}
+
+// --------------------------------------------------------------- class MG
+
+int ubg_mg_create(int width, int height, const float *flag, ubg_mg **out) {
+  return guarded([&] {
+    if (!out) throw ArgError("null argument");
+    if (width < 8 || height < 8) throw ArgError("width and height must be >= 8");
+    check_device();
+    std::unique_ptr<ubg_mg> m(new ubg_mg());
+    m->W = width;
+    m->H = height;
+    UBG_CUDA(cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking));
+    mg_alloc(m->mg, width, height, 1.0f);
+    if (flag) {
+      upload_flag_u8(m->mg.lv[0], flag, width, height, m->st);
+      mg_update_fields(m->mg, m->st);
+    } else {
+      mg_fill_coarse_flags_one(m->mg, m->st);
+    }
+    UBG_CUDA(cudaStreamSynchronize(m->st));
+    *out = m.release();
+    return UBG_OK;
+  });
+}
+
+int ubg_mg_destroy(ubg_mg *m) {
+  return guarded([&] {
+    delete m;
+    return UBG_OK;
+  });
+}
+
+int ubg_mg_update_fields(ubg_mg *m, const float *flag) {
+  return guarded([&] {
+    if (!m || !flag) throw ArgError("null argument");
+    upload_flag_u8(m->mg.lv[0], flag, m->W, m->H, m->st);
+    mg_update_fields(m->mg, m->st);
+    UBG_CUDA(cudaStreamSynchronize(m->st));
+    return UBG_OK;
+  });
+}
+
+int ubg_mg_solve(ubg_mg *m, float *p, const float *f, const float *flag, float h, int zgbc) {
+  return guarded([&] {
+    if (!m || !p || !f || !flag) throw ArgError("null argument");
+    MgLevel &L = m->mg.lv[0];
+    size_t hp = (size_t)m->W * 4, dp = (size_t)L.pitch * 4;
+    upload_flag_u8(L, flag, m->W, m->H, m->st);
+    UBG_CUDA(cudaMemcpy2DAsync(L.e[m->mg.cur0], dp, p, hp, hp, m->H, cudaMemcpyHostToDevice, m->st));
+    UBG_CUDA(cudaMemcpy2DAsync(L.rhs, dp, f, hp, hp, m->H, cudaMemcpyHostToDevice, m->st));
+    mg_set_h(m->mg, h);
+    mg_solve(m->mg, zgbc != 0, m->st);
+    UBG_CUDA(cudaMemcpy2DAsync(p, hp, L.e[m->mg.cur0], dp, hp, m->H, cudaMemcpyDeviceToHost, m->st));
+    UBG_CUDA(cudaStreamSynchronize(m->st));
+    return UBG_OK;
+  });
+}
+
+int ubg_mg_solve_device(ubg_mg *m, float *p, int p_pitch, const float *f, int f_pitch,
+                        const uint8_t *flag, int flag_pitch, float h, int zgbc, void *stream) {
+  return guarded([&] {
+    if (!m || !p || !f || !flag) throw ArgError("null argument");
+    cudaStream_t st = stream ? (cudaStream_t)stream : m->st;
+    MgLevel &L = m->mg.lv[0];
+    size_t w4 = (size_t)m->W * 4, dp = (size_t)L.pitch * 4;
+    UBG_CUDA(cudaMemcpy2DAsync(L.flag, L.pitch, flag, flag_pitch, m->W, m->H, cudaMemcpyDeviceToDevice, st));
+    UBG_CUDA(cudaMemcpy2DAsync(L.e[m->mg.cur0], dp, p, (size_t)p_pitch * 4, w4, m->H,
+                               cudaMemcpyDeviceToDevice, st));
+    UBG_CUDA(cudaMemcpy2DAsync(L.rhs, dp, f, (size_t)f_pitch * 4, w4, m->H, cudaMemcpyDeviceToDevice, st));
+    mg_set_h(m->mg, h);
+    mg_solve(m->mg, zgbc != 0, st);
+    UBG_CUDA(cudaMemcpy2DAsync(p, (size_t)p_pitch * 4, L.e[m->mg.cur0], dp, w4, m->H,
+                               cudaMemcpyDeviceToDevice, st));
+    return UBG_OK;
+  });
+}
+
+// ------------------------------------------------ free solver functions
+
+namespace {
+struct TmpLevel {
+  MgLevel L{};
+  void *mem = nullptr;
+  cudaStream_t st = nullptr;
+  TmpLevel(int w, int h) {
+    L.w = w;
+    L.h = h;
+    L.pitch = round_up(w, 32);
+    size_t n = (size_t)L.pitch * h;
+    size_t fb = (n * 4 + 255) / 256 * 256;
+    if (cudaMalloc(&mem, 3 * fb + n + 256) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    char *p = (char *)mem;
+    L.e[0] = (float *)p; p += fb;
+    L.e[1] = (float *)p; p += fb;
+    L.rhs = (float *)p; p += fb;
+    L.flag = (uint8_t *)p;
+    UBG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    UBG_CUDA(cudaMemsetAsync(mem, 0, 3 * fb + n + 256, st));
+  }
+  ~TmpLevel() {
+    if (st) cudaStreamSynchronize(st);
+    if (mem) cudaFree(mem);
+    if (st) cudaStreamDestroy(st);
+  }
+  void load(const float *p, const float *f, const float *flag) {
+    size_t hp = (size_t)L.w * 4, dp = (size_t)L.pitch * 4;
+    if (p) UBG_CUDA(cudaMemcpy2DAsync(L.e[0], dp, p, hp, hp, L.h, cudaMemcpyHostToDevice, st));
+    UBG_CUDA(cudaMemcpy2DAsync(L.rhs, dp, f, hp, hp, L.h, cudaMemcpyHostToDevice, st));
+    upload_flag_u8(L, flag, L.w, L.h, st);
+  }
+};
+}  // namespace
+
+int ubg_rbgs(float *p, const float *f, const float *flag, int width, int height, float h,
+             float alpha) {
+  return guarded([&] {
+    if (!p || !f || !flag) throw ArgError("null argument");
+    if (width < 3 || height < 3) throw ArgError("grid too small");
+    check_device();
+    TmpLevel t(width, height);
+    t.L.hh = h;
+    t.load(p, f, flag);
+    int cur = 0;
+    level_rbgs(t.L, cur, alpha, t.st);
+    size_t hp = (size_t)width * 4, dp = (size_t)t.L.pitch * 4;
+    UBG_CUDA(cudaMemcpy2DAsync(p, hp, t.L.e[cur], dp, hp, height, cudaMemcpyDeviceToHost, t.st));
+    UBG_CUDA(cudaStreamSynchronize(t.st));
+    return UBG_OK;
+  });
+}
+
+int ubg_residual(const float *p, const float *f, const float *flag, float *r, int width, int height,
+                 float h, double *l2norm) {
+  return guarded([&] {
+    if (!p || !f || !flag) throw ArgError("null argument");
+    if (width < 3 || height < 3) throw ArgError("grid too small");
+    check_device();
+    TmpLevel t(width, height);
+    t.L.hh = h;
+    t.load(p, f, flag);
+    double *dn = nullptr;
+    UBG_CUDA(cudaMallocAsync((void **)&dn, sizeof(double), t.st));
+    UBG_CUDA(cudaMemsetAsync(dn, 0, sizeof(double), t.st));
+    level_residual(t.L, 0, t.L.e[1], dn, t.st);
+    double nh = 0.0;
+    UBG_CUDA(cudaMemcpyAsync(&nh, dn, sizeof(double), cudaMemcpyDeviceToHost, t.st));
+    size_t hp = (size_t)width * 4, dp = (size_t)t.L.pitch * 4;
+    if (r) UBG_CUDA(cudaMemcpy2DAsync(r, hp, t.L.e[1], dp, hp, height, cudaMemcpyDeviceToHost, t.st));
+    UBG_CUDA(cudaFreeAsync(dn, t.st));
+    UBG_CUDA(cudaStreamSynchronize(t.st));
+    if (l2norm) *l2norm = std::sqrt(nh);
+    return UBG_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,198 @@
+// Internal declarations of the ubootgl_gb300 CUDA library.
+//
+// Device layout (one simulation of W x H pressure cells):
+//   every level-0 field is a pitched, row-major float array with row pitch
+//   P = round_up(W, 32) elements (128-byte rows); vx uses columns 0..W-2 of
+//   H rows, vy columns 0..W-1 of H-1 rows.  The flag is one byte per cell
+//   with the same element pitch.  Coarse multigrid levels have their own
+//   pitch round_up(w_l, 32).
+//
+// Arithmetic: the library is compiled with -fmad=false; every kernel
+// evaluates the reference's expressions in the reference's source order in
+// IEEE float, with explicit __fmaf_rn only in the Catmull-Rom sampler.  That
+// is what makes the FP32 path bit-identical to the CPU restatement of the
+// reference used as the test oracle.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ubootgl_gb300.h"
+
+namespace ubg {
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct ArgError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define UBG_CUDA(call)                                                                    \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      throw ::ubg::CudaError(std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + \
+                             __FILE__ + ":" + std::to_string(__LINE__) + ")");           \
+  } while (0)
+
+#define UBG_LAUNCH_CHECK() UBG_CUDA(cudaGetLastError())
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// ------------------------------------------------------------ step scalars
+// Quantities that depend on dt, formed exactly as the reference forms them
+// (simulation.cpp:105, 165, 242, 276, 286) in float.  They live in device
+// memory so that a captured step graph does not depend on dt.
+struct StepScalars {
+  float dt;
+  float a;      // dt * mu * (width - 1.0f) / pwidth
+  float den;    // 1.0f + 4.0f * a
+  float ih;     // 1.0f / h
+  float chalf;  // 0.5f * dt * ih
+  float cfull;  // dt * ih
+};
+
+struct SinkCell {
+  int x, y;
+  float v;
+};
+
+// Boundary types per edge, order West, East, North, South.
+struct Bcs {
+  int w, e, n, s;
+};
+
+// ------------------------------------------------------------- kernels
+// Velocity fields of one simulation, for the step kernels.
+struct VelBufs {
+  float *vx[2];
+  float *vy[2];
+  int pitch, W, H;
+};
+
+// setVBCs (simulation.cpp:80-102): boundary values computed from the front
+// buffers (fx, fy), written to both buffers of each component.
+void launch_vbc(const VelBufs &v, int fx, int fy, Bcs bc, bool do_vx, bool do_vy,
+                cudaStream_t st);
+// applyAccumulatedVelocity (simulation.cpp:376-396).
+void launch_accum(const VelBufs &v, int fx, int fy, float *ax, float *ay, cudaStream_t st);
+// One Jacobi diffusion sweep, buffer src -> buffer 1-src of each component
+// (simulation.cpp:112-129, 138-155); comps bit 0 = vx, bit 1 = vy.
+void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const uint8_t *flag,
+                          const StepScalars *sc, int comps, cudaStream_t st);
+// advect (simulation.cpp:241-354): reads buffer `src` of vx / vy, writes the
+// advected faces into buffer 1-src (faces the reference does not advect keep
+// their value).
+void launch_advect(const VelBufs &v, int srcx, int srcy, const uint8_t *flag,
+                   const StepScalars *sc, cudaStream_t st);
+// Divergence into f (simulation.cpp:166-171).
+void launch_divergence(const VelBufs &v, int fx, int fy, float *f, const StepScalars *sc,
+                       cudaStream_t st);
+// Sinks (simulation.cpp:173-183), already resolved to cells on the host.
+void launch_sinks(float *f, int pitch, const SinkCell *cells, int n, cudaStream_t st);
+// setPBC (simulation.cpp:36-45).
+void launch_pbc(float *p, int pitch, int W, int H, Bcs bc, cudaStream_t st);
+// Pressure-gradient update (simulation.cpp:196-207).
+void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const uint8_t *flag,
+                     const StepScalars *sc, cudaStream_t st);
+// max(|vx|, |vy|) over the front buffers -> dt = cfl*h/max (extension) and
+// the derived scalars.
+void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, float pwidth,
+                unsigned int *umax_bits, StepScalars *sc, cudaStream_t st);
+
+// ------------------------------------------------------------ multigrid
+struct MgLevel {
+  int w, h, pitch;
+  float hh;            // grid spacing of this level
+  uint8_t *flag;       // w x h, pitched
+  float *e[2];         // level 0: pressure ping-pong; coarse: error ping-pong
+  float *rhs;          // level 0: f; coarse: restricted residual
+};
+
+struct MgHier {
+  int levels = 0;
+  std::vector<MgLevel> lv;
+  int cur0 = 0;                  // which e[] of level 0 holds p
+  void *arena = nullptr;
+  size_t arena_bytes = 0;
+  double *norm = nullptr;        // device scalar for residual norms
+  // profiling hooks (optional)
+  cudaEvent_t ev_pair[2] = {nullptr, nullptr};
+};
+
+// Allocates the hierarchy for a W x H level-0 grid with spacing h0.
+void mg_alloc(MgHier &mg, int W, int H, float h0);
+void mg_free(MgHier &mg);
+// MG::updateFields on the device: level 0 flag must already be set.
+void mg_update_fields(MgHier &mg, cudaStream_t st);
+// Sets all coarse flags to 1.0 (MG(width, height) without a flag).
+void mg_fill_coarse_flags_one(MgHier &mg, cudaStream_t st);
+// One call of MG::solve(p, f, flag, h, zgbc) on level 0's e[cur0] / rhs.
+void mg_solve(MgHier &mg, bool zgbc, cudaStream_t st);
+// Recomputes every level's spacing from the level-0 spacing h0
+// (h * (w-1) / (wc-1) per level, pressure_solver.cpp:225).
+void mg_set_h(MgHier &mg, float h0);
+// One red-black sweep of a single level (free function rbgs), e[cur] -> e[1-cur].
+void level_rbgs(MgLevel &L, int &cur, float alpha, cudaStream_t st);
+// Residual field of one level into `r` (pitched like the level, may be null)
+// with its squared L2 norm accumulated into *norm2 (device double, may be null).
+void level_residual(const MgLevel &L, int cur, float *r, double *norm2, cudaStream_t st);
+
+// Counters for the benchmark.
+struct LaunchStats {
+  long launches = 0;
+};
+extern thread_local LaunchStats g_stats;
+
+// Optional per-kernel timing: when a Profiler is installed for the calling
+// thread (profiling mode, never during graph capture), every launch site
+// records a CUDA event pair on its stream, tagged with its kernel class.
+enum KernelClass {
+  KC_VBC = 0, KC_ACCUM, KC_DIFFUSE, KC_ADVECT, KC_DIVERGENCE, KC_SINKS, KC_PBC, KC_GRADIENT,
+  KC_CFL, KC_SMOOTH_L0, KC_SMOOTH_COARSE, KC_RESTRICT_L0, KC_RESTRICT_COARSE, KC_COARSEN,
+  KC_RESIDUAL, KC_TRACERS, KC_OTHER, KC_COUNT
+};
+const char *kernel_class_name(int kc);
+
+struct Profiler {
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  struct Mark {
+    int kc;
+    size_t a, b;
+  };
+  std::vector<Mark> marks;
+  double total_ms[KC_COUNT] = {};
+  long count[KC_COUNT] = {};
+  cudaEvent_t next();
+  void collect();  // after the stream is synchronised
+  ~Profiler();
+};
+extern thread_local Profiler *g_prof;
+
+struct ProfScope {
+  Profiler *p;
+  size_t a = 0;
+  int kc;
+  cudaStream_t st;
+  ProfScope(int kc_, cudaStream_t st_) : p(g_prof), kc(kc_), st(st_) {
+    if (p) {
+      a = p->used;
+      cudaEventRecord(p->next(), st);
+    }
+  }
+  ~ProfScope() {
+    if (p) {
+      size_t b = p->used;
+      cudaEventRecord(p->next(), st);
+      p->marks.push_back({kc, a, b});
+    }
+  }
+};
+
+}  // namespace ubg

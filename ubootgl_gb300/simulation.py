@@ -1,0 +1,258 @@
+"""Python mirror of the reference's Simulation and MG classes over the C ABI.
+
+class Simulation   -- simulation.hpp:18-141 (constructor from a flag grid,
+                      step, the stage methods, the public fields).
+class MG           -- pressure_solver.hpp:13-76 (MG(width, height), MG(flag),
+                      updateFields, solve).
+rbgs, calculateResidualField -- the free functions of pressure_solver.hpp.
+
+Fields are numpy float32 arrays indexed [y, x] (row-major, idx = y*width+x as
+in db2dgrid.hpp:19).  Reads download from the device; assignments upload.
+All compute runs in the CUDA library; there is no CPU path.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None and a.shape != shape:
+        raise ValueError("expected shape %s, got %s" % (shape, a.shape))
+    return a
+
+
+class Simulation:
+    """Simulation(flag, pwidth, mu), simulation.hpp:32-67."""
+
+    BC = L.BC
+
+    def __init__(self, flag, pwidth=1.0, mu=1e-4):
+        self._lib = L.load()
+        flag = _f32(flag)
+        self.height, self.width = flag.shape
+        self.pwidth = float(np.float32(pwidth))
+        self.mu = float(np.float32(mu))
+        h = C.c_void_p()
+        L.check(self._lib.ubg_create(L.fptr(flag), self.width, self.height, pwidth, mu,
+                                     C.byref(h)))
+        self._h = h
+        self.dt = 0.0
+        # h = pwidth / (width - 1.0f), simulation.hpp:63
+        self.h = float(np.float32(pwidth) / (np.float32(self.width) - np.float32(1.0)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ubg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------ options
+    def set_options(self, solver_mode=None, vcycles=None, tol=None, max_vcycles=None,
+                    use_graph=None):
+        o = L.Options()
+        L.check(self._lib.ubg_default_options(C.byref(o)))
+        cur = getattr(self, "_opts", None)
+        if cur is not None:
+            o = cur
+        if solver_mode is not None:
+            o.solver_mode = solver_mode
+        if vcycles is not None:
+            o.vcycles = vcycles
+        if tol is not None:
+            o.tol = tol
+        if max_vcycles is not None:
+            o.max_vcycles = max_vcycles
+        if use_graph is not None:
+            o.use_graph = int(use_graph)
+        L.check(self._lib.ubg_set_options(self._h, C.byref(o)))
+        self._opts = o
+
+    def set_bcs(self, west="INFLOW", east="OUTFLOW_ZERO_PRESSURE", north="NOSLIP",
+                south="NOSLIP"):
+        L.check(self._lib.ubg_set_bcs(self._h, L.BC[west], L.BC[east], L.BC[north],
+                                      L.BC[south]))
+
+    # ------------------------------------------------------------ the step
+    def step(self, timestep):
+        """Simulation::step, simulation.cpp:356-374."""
+        self.dt = timestep
+        L.check(self._lib.ubg_step(self._h, timestep))
+
+    def step_cfl(self, cfl=0.5):
+        L.check(self._lib.ubg_step_cfl(self._h, cfl))
+
+    def last_dt(self):
+        v = C.c_float()
+        L.check(self._lib.ubg_last_dt(self._h, C.byref(v)))
+        return v.value
+
+    def applyAccumulatedVelocity(self):
+        L.check(self._lib.ubg_apply_accumulated_velocity(self._h))
+
+    def diffuse(self):
+        L.check(self._lib.ubg_diffuse(self._h, self.dt))
+
+    def advect(self):
+        L.check(self._lib.ubg_advect(self._h, self.dt))
+
+    def setVBCs(self):
+        L.check(self._lib.ubg_set_vbcs(self._h))
+
+    def setPBC(self):
+        L.check(self._lib.ubg_set_pbc(self._h))
+
+    def project(self):
+        L.check(self._lib.ubg_project(self._h, self.dt))
+
+    def add_sink(self, x, y, strength):
+        """sinks.push_back(glm::vec3(x, y, strength))."""
+        L.check(self._lib.ubg_add_sink(self._h, x, y, strength))
+
+    def mg_solve(self, zero_gradient_bc=True):
+        L.check(self._lib.ubg_mg_solve_sim(self._h, int(zero_gradient_bc)))
+
+    def sync(self):
+        L.check(self._lib.ubg_sync(self._h))
+
+    # ------------------------------------------------------------- fields
+    def _shape(self, name):
+        W, H = self.width, self.height
+        if name.startswith("vx"):
+            return (H, W - 1)
+        if name.startswith("vy"):
+            return (H - 1, W)
+        return (H, W)
+
+    def get(self, name):
+        out = np.empty(self._shape(name), dtype=np.float32)
+        L.check(self._lib.ubg_download(self._h, L.FIELDS[name], L.fptr(out)))
+        return out
+
+    def set(self, name, arr):
+        a = _f32(arr, self._shape(name))
+        L.check(self._lib.ubg_upload(self._h, L.FIELDS[name], L.fptr(a)))
+
+    def update_flag(self, flag):
+        """memcpy(sim.flag.data(), ...) + sim.mg.updateFields(sim.flag)."""
+        self.set("flag", flag)
+
+    def mg_levels(self):
+        n = C.c_int()
+        L.check(self._lib.ubg_mg_levels(self._h, C.byref(n)))
+        return n.value
+
+    def mg_level_flag(self, level):
+        w, h = C.c_int(), C.c_int()
+        L.check(self._lib.ubg_mg_level_flag(self._h, level, C.byref(w), C.byref(h), None))
+        out = np.empty((h.value, w.value), dtype=np.float32)
+        L.check(self._lib.ubg_mg_level_flag(self._h, level, None, None, L.fptr(out)))
+        return out
+
+    def device_field(self, name):
+        """(device pointer, pitch in elements, width, height) of a field."""
+        ptr, pitch, w, h = C.c_void_p(), C.c_int(), C.c_int(), C.c_int()
+        L.check(self._lib.ubg_field_device(self._h, L.FIELDS[name], C.byref(ptr), C.byref(pitch),
+                                           C.byref(w), C.byref(h)))
+        return ptr.value, pitch.value, w.value, h.value
+
+    def profile(self, on=True):
+        L.check(self._lib.ubg_profile_enable(self._h, int(on)))
+
+    def profile_reset(self):
+        L.check(self._lib.ubg_profile_reset(self._h))
+
+    def profile_classes(self):
+        """{kernel class: (total ms, launches)} accumulated while profiling."""
+        out = {}
+        for kc in range(17):
+            name, ms, n = C.c_char_p(), C.c_double(), C.c_int()
+            L.check(self._lib.ubg_profile_class(self._h, kc, C.byref(name), C.byref(ms),
+                                                C.byref(n)))
+            if n.value:
+                out[name.value.decode()] = (ms.value, n.value)
+        return out
+
+    def profile_read(self):
+        sm, sl, st, kl = C.c_double(), C.c_int(), C.c_double(), C.c_int()
+        L.check(self._lib.ubg_profile_read(self._h, C.byref(sm), C.byref(sl), C.byref(st),
+                                           C.byref(kl)))
+        return {"smoother_ms": sm.value, "smoother_launches": sl.value, "step_ms": st.value,
+                "kernel_launches": kl.value}
+
+    vx = property(lambda s: s.get("vx"), lambda s, a: s.set("vx", a))
+    vy = property(lambda s: s.get("vy"), lambda s, a: s.set("vy", a))
+    p = property(lambda s: s.get("p"), lambda s, a: s.set("p", a))
+    f = property(lambda s: s.get("f"), lambda s, a: s.set("f", a))
+    flag = property(lambda s: s.get("flag"), lambda s, a: s.set("flag", a))
+    vx_current = property(lambda s: s.get("vx_current"))
+    vy_current = property(lambda s: s.get("vy_current"))
+
+
+class MG:
+    """class MG, pressure_solver.hpp:13-76.  MG(width, height) or MG(flag)."""
+
+    def __init__(self, width_or_flag, height=None):
+        self._lib = L.load()
+        h = C.c_void_p()
+        if height is None:
+            flag = _f32(width_or_flag)
+            self.height, self.width = flag.shape
+            L.check(self._lib.ubg_mg_create(self.width, self.height, L.fptr(flag), C.byref(h)))
+        else:
+            self.width, self.height = int(width_or_flag), int(height)
+            L.check(self._lib.ubg_mg_create(self.width, self.height, None, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.ubg_mg_destroy(self._h)
+            self._h = None
+
+    def updateFields(self, flag):
+        L.check(self._lib.ubg_mg_update_fields(self._h, L.fptr(_f32(flag))))
+
+    def solve(self, p, f, flag, h, zeroGradientBC=False):
+        """MG::solve: updates p (a float32 array) in place and returns it."""
+        shape = (self.height, self.width)
+        if not (isinstance(p, np.ndarray) and p.dtype == np.float32 and p.flags.c_contiguous
+                and p.shape == shape):
+            raise ValueError("p must be a C-contiguous float32 array of shape %s" % (shape,))
+        L.check(self._lib.ubg_mg_solve(self._h, L.fptr(p), L.fptr(_f32(f, shape)),
+                                       L.fptr(_f32(flag, shape)), h, int(zeroGradientBC)))
+        return p
+
+
+def rbgs(p, f, flag, h, alpha=1.0):
+    """rbgs(p, f, flag, h, alpha), pressure_solver.cpp:35-89; returns the new p."""
+    lib = L.load()
+    p = _f32(p).copy()
+    H, W = p.shape
+    L.check(lib.ubg_rbgs(L.fptr(p), L.fptr(_f32(f, (H, W))), L.fptr(_f32(flag, (H, W))), W, H,
+                         h, alpha))
+    return p
+
+
+def calculateResidualField(p, f, flag, h):
+    """calculateResidualField, pressure_solver.cpp:91-116 -> (r, ||r||_2)."""
+    lib = L.load()
+    p = _f32(p)
+    H, W = p.shape
+    r = np.zeros((H, W), dtype=np.float32)
+    n = C.c_double()
+    L.check(lib.ubg_residual(L.fptr(p), L.fptr(_f32(f, (H, W))), L.fptr(_f32(flag, (H, W))),
+                             L.fptr(r), W, H, h, C.byref(n)))
+    return r, n.value

@@ -79,9 +79,13 @@ def initial_velocity(flag, seed=1, amp=0.1, sigma=8.0, u_in=1.0):
 
 
 def cfl_dt(vx, vy, h, cfl=0.5):
-    """dt = cfl * h / max|u| over both staggered components (float32)."""
-    umax = max(float(np.abs(vx).max()), float(np.abs(vy).max()), 1e-7)
-    return np.float32(cfl * h / umax)
+    """dt = cfl * h / max|u| over both staggered components, in float32
+    arithmetic ((cfl * h) / umax with umax >= 1e-7), which is what the
+    device-side CFL step computes."""
+    f = np.float32
+    umax = max(f(np.abs(vx).max()), f(np.abs(vy).max()))
+    umax = umax if umax > f(1e-7) else f(1e-7)
+    return f(f(f(cfl) * f(h)) / umax)
 
 
 def grid_h(W, pwidth=1.0):
