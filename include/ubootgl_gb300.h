@@ -174,7 +174,7 @@ int ubg_sync(ubg_sim *sim);
  * kernel; ubg_profile_read gives the mean level-0 smoother launch time, the
  * mean profiled step time and the launch count of the last step;
  * ubg_profile_class gives the accumulated time and launch count of one
- * kernel class (0 <= kc < 17, name returned). */
+ * kernel class (0 <= kc < 19, name returned). */
 int ubg_profile_enable(ubg_sim *sim, int on);
 int ubg_profile_read(ubg_sim *sim, double *smoother_ms, int *smoother_launches,
                      double *step_ms, int *kernel_launches);

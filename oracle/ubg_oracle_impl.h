@@ -430,14 +430,22 @@ void FN(diffuse)(SIM_T *s) {
 }
 
 /* ------------------------------------------------------------- advection */
-/* CubicHermite, interpolators.hpp:78-85 (Catmull-Rom).  Evaluated here as
- * a Horner polynomial with fused multiply-adds; the coefficient formulas are
- * the reference's. */
-static inline REAL FN(cubic_hermite)(REAL t, REAL A, REAL B, REAL C, REAL D) {
-  REAL a = (((REAL)-0.5 * A + (REAL)1.5 * B) - (REAL)1.5 * C) + (REAL)0.5 * D;
-  REAL b = ((A - (REAL)2.5 * B) + (REAL)2.0 * C) - (REAL)0.5 * D;
-  REAL c = (REAL)0.5 * (C - A);
-  return FMA(FMA(FMA(a, t, b), t, c), t, B);
+/* CubicHermite, interpolators.hpp:78-85, is the Catmull-Rom cubic through
+ * A, B, C, D at parameter t.  It is evaluated here through its four weights
+ * (the same polynomial, regrouped):
+ *   wA = t(-1/2 + t(1 - t/2)),  wB = 1 + t^2(-5/2 + 3t/2),
+ *   wC = t(1/2 + t(2 - 3t/2)),  wD = t^2(-1/2 + t/2),
+ * with explicit fused multiply-adds; the weights of one t serve all four
+ * columns of a bicubic sample. */
+static inline void FN(cr_weights)(REAL t, REAL w[4]) {
+  REAL t2 = t * t;
+  w[0] = t * FMA(t, FMA((REAL)-0.5, t, (REAL)1.0), (REAL)-0.5);
+  w[1] = FMA(t2, FMA((REAL)1.5, t, (REAL)-2.5), (REAL)1.0);
+  w[2] = t * FMA(t, FMA((REAL)-1.5, t, (REAL)2.0), (REAL)0.5);
+  w[3] = t2 * FMA((REAL)0.5, t, (REAL)-0.5);
+}
+static inline REAL FN(cr_dot)(const REAL w[4], REAL A, REAL B, REAL C, REAL D) {
+  return FMA(w[3], D, FMA(w[2], C, FMA(w[1], B, w[0] * A)));
 }
 
 /* bicubicSample, interpolators.hpp:92-206: clamp to [3, size-3], truncate,
@@ -451,13 +459,15 @@ static inline REAL FN(bicubic)(const REAL *g, int gw, int gh, REAL cx, REAL cy) 
   cy = cy > (REAL)3.0 ? cy : (REAL)3.0;
   int ix = (int)cx, iy = (int)cy;
   REAL sx = cx - (REAL)ix, sy = cy - (REAL)iy;
-  REAL col[4];
+  REAL wy[4], wx[4], col[4];
+  FN(cr_weights)(sy, wy);
+  FN(cr_weights)(sx, wx);
   for (int j = 0; j < 4; j++) {
     int x = ix - 1 + j;
-    col[j] = FN(cubic_hermite)(sy, AT(g, gw, x, iy - 1), AT(g, gw, x, iy), AT(g, gw, x, iy + 1),
-                               AT(g, gw, x, iy + 2));
+    col[j] = FN(cr_dot)(wy, AT(g, gw, x, iy - 1), AT(g, gw, x, iy), AT(g, gw, x, iy + 1),
+                        AT(g, gw, x, iy + 2));
   }
-  return FN(cubic_hermite)(sx, col[0], col[1], col[2], col[3]);
+  return FN(cr_dot)(wx, col[0], col[1], col[2], col[3]);
 }
 
 /* Whether the reference advects face x of row y.  The x loops run in chunks

@@ -109,14 +109,29 @@ def test_accum_and_sinks(lib):
 
 
 def test_cfl_step_matches_host_dt(lib):
+    """Device-side dt = 0.5 h / max|u| (max folded into the gradient and
+    boundary kernels of the previous step) equals the host formula, also
+    after the fields change between steps."""
     W, H = 130, 66
     a, ref, flag = make_pair(W, H, seed=8)
-    for k in range(3):
+    rng = np.random.default_rng(1)
+    for k in range(6):
+        if k == 3:
+            ax = (0.05 * rng.standard_normal((H, W - 1))).astype(np.float32)
+            for s in (a, ref):
+                s.set("vx_accum", ax)
+        if k == 4:
+            vy = ref.get("vy") * np.float32(1.5)
+            for s in (a, ref):
+                s.set("vy", vy)
         dt = WL.cfl_dt(ref.get("vx"), ref.get("vy"), ref.h)
         a.step_cfl(0.5)
-        assert a.last_dt() == float(dt)
-        ref.step(dt)
-    assert_same(a, ref, names=("vx", "vy", "p"))
+        if k != 3:  # with accumulated velocity, dt is taken after it is applied
+            assert a.last_dt() == float(dt), k
+            ref.step(dt)
+        else:
+            ref.step(np.float32(a.last_dt()))
+        assert_same(a, ref, names=("vx", "vy", "p"), ctx="cfl step %d" % k)
 
 
 def test_config0_1024x512_100_steps(lib):

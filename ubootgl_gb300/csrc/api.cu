@@ -87,6 +87,7 @@ struct ubg_sim {
   VelBufs v{};
   int fx = 0, fy = 0;
   float *ax = nullptr, *ay = nullptr;
+  uint8_t *codes_x = nullptr, *codes_y = nullptr;
   MgHier mg;
   StepScalars *d_sc = nullptr;
   unsigned int *d_umax = nullptr;
@@ -101,6 +102,7 @@ struct ubg_sim {
   std::vector<HostSink> sinks;
   std::vector<float> flag_host;
   bool accum_dirty = false;
+  bool umax_ready = false;  // d_umax holds max|u| of the current fields
   float last_dt = 0.0f;
   int last_vcycles = 0;
   // CUDA graph of the fixed-cycle step body
@@ -159,7 +161,7 @@ struct ubg_sim {
   void diffuse() {
     launch_vbc(v, fx, fy, bc, false, true, st);
     for (int i = 0; i < 2; i++) {
-      launch_diffuse_sweep(v, fx, fy, flag(), d_sc, 3, st);
+      launch_diffuse_sweep(v, fx, fy, d_sc, 3, st);
       fx ^= 1;
       fy ^= 1;
       set_vbcs();
@@ -167,7 +169,7 @@ struct ubg_sim {
   }
 
   void advect() {
-    launch_advect(v, fx, fy, flag(), d_sc, st);
+    launch_advect(v, fx, fy, d_sc, st);
     fx ^= 1;
     fy ^= 1;
   }
@@ -211,9 +213,12 @@ struct ubg_sim {
     level_residual_of_rhs(L0, &fnorm2);
     double target2 = (double)opt.tol * (double)opt.tol * fnorm2;
     for (c = 0; c < opt.max_vcycles; c++) {
-      mg_solve(mg, true, st);
+      // the level-0 post-smoothing launch returns ||r||^2 of its result
       UBG_CUDA(cudaMemsetAsync(mg.norm, 0, sizeof(double), st));
-      level_residual(L0, mg.cur0, nullptr, mg.norm, st);
+      mg.post_norm2 = mg.levels > 2 ? mg.norm : nullptr;
+      mg_solve(mg, true, st);
+      mg.post_norm2 = nullptr;
+      if (mg.levels <= 2) level_residual(L0, mg.cur0, nullptr, mg.norm, st);
       UBG_CUDA(cudaMemcpyAsync(h_norm, mg.norm, sizeof(double), cudaMemcpyDeviceToHost, st));
       UBG_CUDA(cudaStreamSynchronize(st));
       if (*h_norm <= target2) {
@@ -237,26 +242,30 @@ struct ubg_sim {
   }
 
   // project(), simulation.cpp:164-208 (without the trailing setVBCs of step).
+  // The gradient kernel also starts the max|u| reduction for the next CFL dt.
   void project(int nsink_cells) {
     launch_divergence(v, fx, fy, f(), d_sc, st);
     launch_sinks(f(), P, d_sinks, nsink_cells, st);
     solve_pressure();
     launch_pbc(p(), P, W, H, bc, st);
-    launch_gradient(v, fx, fy, p(), flag(), d_sc, st);
+    UBG_CUDA(cudaMemsetAsync(d_umax, 0, sizeof(unsigned int), st));
+    launch_gradient(v, fx, fy, p(), d_sc, d_umax, st);
   }
 
   // Everything of step() after the scalars are staged and the accumulated
-  // velocity is applied; captured into a graph in fixed-cycle mode.
+  // velocity is applied; captured into a graph in fixed-cycle mode.  The
+  // final setVBCs completes max|u| over all faces.
   void step_body(int nsink_cells) {
     diffuse();
     advect();
     set_vbcs();
     project(nsink_cells);
-    set_vbcs();
+    launch_vbc(v, fx, fy, bc, true, true, st, d_umax);
   }
 
   void step(float dt, bool device_dt, float cfl) {
     long l0 = g_stats.launches;
+    bool accum_dirty_at_start = accum_dirty;
     struct ProfInstall {
       bool on;
       ProfInstall(bool on_, Profiler *p) : on(on_) {
@@ -270,7 +279,7 @@ struct ubg_sim {
     if (accum_dirty) apply_accum();
     int nsc = 0;
     if (device_dt) {
-      launch_cfl(v, fx, fy, cfl, h, mu, pwidth, d_umax, d_sc, st);
+      launch_cfl(v, fx, fy, cfl, h, mu, pwidth, d_umax, d_sc, st, umax_ready && !accum_dirty_at_start);
     } else {
       push_scalars(dt);
       nsc = sinks.empty() ? 0 : stage_sinks(dt);
@@ -287,6 +296,7 @@ struct ubg_sim {
     } else {
       step_body(nsc);
     }
+    umax_ready = true;
     if (prof) {
       UBG_CUDA(cudaEventRecord(ev_step[1], st));
       // per-step collection keeps the event pool small
@@ -453,8 +463,9 @@ int ubg_create(const float *flag, int width, int height, float pwidth, float mu,
     UBG_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
     size_t n = (size_t)s->P * height;
     size_t fb = (n * 4 + 255) / 256 * 256;
+    size_t bb = (n + 255) / 256 * 256;
     size_t extra = 256 * 3 + (size_t)kMaxSinks * 9 * sizeof(SinkCell);
-    size_t total = 6 * fb + extra;
+    size_t total = 6 * fb + 2 * bb + extra;
     if (cudaMalloc(&s->arena, total) != cudaSuccess) {
       cudaGetLastError();
       throw std::bad_alloc();
@@ -467,6 +478,10 @@ int ubg_create(const float *flag, int width, int height, float pwidth, float mu,
     s->v.vy[1] = (float *)p; p += fb;
     s->ax = (float *)p; p += fb;
     s->ay = (float *)p; p += fb;
+    s->codes_x = (uint8_t *)p; p += bb;
+    s->codes_y = (uint8_t *)p; p += bb;
+    s->v.cx = s->codes_x;
+    s->v.cy = s->codes_y;
     s->d_sc = (StepScalars *)p; p += 256;
     s->d_umax = (unsigned int *)p; p += 256;
     p += 256;
@@ -484,6 +499,7 @@ int ubg_create(const float *flag, int width, int height, float pwidth, float mu,
     s->flag_host.assign(flag, flag + (size_t)width * height);
     upload_flag_u8(s->mg.lv[0], flag, width, height, s->st);
     mg_update_fields(s->mg, s->st);
+    launch_face_codes(s->v, s->flag(), s->codes_x, s->codes_y, s->st);
     // vy(x, 0) = 0 and vx(0, y) = 1 in both buffers (simulation.hpp:55-60)
     std::vector<float> col((size_t)height, 1.0f);
     for (int b = 0; b < 2; b++)
@@ -558,6 +574,7 @@ int ubg_last_dt(ubg_sim *s, float *dt) {
 int ubg_apply_accumulated_velocity(ubg_sim *s) {
   return guarded([&] {
     if (!s) throw ArgError("null handle");
+    s->umax_ready = false;
     s->apply_accum();
     return UBG_OK;
   });
@@ -566,6 +583,7 @@ int ubg_apply_accumulated_velocity(ubg_sim *s) {
 int ubg_diffuse(ubg_sim *s, float dt) {
   return guarded([&] {
     if (!s) throw ArgError("null handle");
+    s->umax_ready = false;
     s->push_scalars(dt);
     s->diffuse();
     return UBG_OK;
@@ -575,6 +593,7 @@ int ubg_diffuse(ubg_sim *s, float dt) {
 int ubg_advect(ubg_sim *s, float dt) {
   return guarded([&] {
     if (!s) throw ArgError("null handle");
+    s->umax_ready = false;
     s->push_scalars(dt);
     s->advect();
     return UBG_OK;
@@ -584,6 +603,7 @@ int ubg_advect(ubg_sim *s, float dt) {
 int ubg_set_vbcs(ubg_sim *s) {
   return guarded([&] {
     if (!s) throw ArgError("null handle");
+    s->umax_ready = false;
     s->set_vbcs();
     return UBG_OK;
   });
@@ -600,6 +620,7 @@ int ubg_set_pbc(ubg_sim *s) {
 int ubg_project(ubg_sim *s, float dt) {
   return guarded([&] {
     if (!s) throw ArgError("null handle");
+    s->umax_ready = false;
     s->push_scalars(dt);
     int n = s->sinks.empty() ? 0 : s->stage_sinks(dt);
     s->project(n);
@@ -619,10 +640,12 @@ int ubg_add_sink(ubg_sim *s, float x, float y, float strength) {
 int ubg_upload(ubg_sim *s, int field, const float *src) {
   return guarded([&] {
     if (!s || !src) throw ArgError("null argument");
+    s->umax_ready = false;
     if (field == UBG_FLAG) {
       upload_flag_u8(s->mg.lv[0], src, s->W, s->H, s->st);
       s->flag_host.assign(src, src + (size_t)s->W * s->H);
       mg_update_fields(s->mg, s->st);
+      launch_face_codes(s->v, s->flag(), s->codes_x, s->codes_y, s->st);
       s->sync();
       return UBG_OK;
     }
@@ -688,6 +711,7 @@ int ubg_mg_solve_sim(ubg_sim *s, int zgbc) {
 int ubg_field_device(ubg_sim *s, int field, void **ptr, int *pitch, int *w, int *h) {
   return guarded([&] {
     if (!s || !ptr) throw ArgError("null argument");
+    s->umax_ready = false;
     if (field == UBG_FLAG) {
       *ptr = s->flag();
       if (pitch) *pitch = s->P;
@@ -811,6 +835,7 @@ int ubg_mg_solve(ubg_mg *m, float *p, const float *f, const float *flag, float h
     MgLevel &L = m->mg.lv[0];
     size_t hp = (size_t)m->W * 4, dp = (size_t)L.pitch * 4;
     upload_flag_u8(L, flag, m->W, m->H, m->st);
+    level_make_code(L, m->st);
     UBG_CUDA(cudaMemcpy2DAsync(L.e[m->mg.cur0], dp, p, hp, hp, m->H, cudaMemcpyHostToDevice, m->st));
     UBG_CUDA(cudaMemcpy2DAsync(L.rhs, dp, f, hp, hp, m->H, cudaMemcpyHostToDevice, m->st));
     mg_set_h(m->mg, h);
@@ -829,6 +854,7 @@ int ubg_mg_solve_device(ubg_mg *m, float *p, int p_pitch, const float *f, int f_
     MgLevel &L = m->mg.lv[0];
     size_t w4 = (size_t)m->W * 4, dp = (size_t)L.pitch * 4;
     UBG_CUDA(cudaMemcpy2DAsync(L.flag, L.pitch, flag, flag_pitch, m->W, m->H, cudaMemcpyDeviceToDevice, st));
+    level_make_code(L, st);
     UBG_CUDA(cudaMemcpy2DAsync(L.e[m->mg.cur0], dp, p, (size_t)p_pitch * 4, w4, m->H,
                                cudaMemcpyDeviceToDevice, st));
     UBG_CUDA(cudaMemcpy2DAsync(L.rhs, dp, f, (size_t)f_pitch * 4, w4, m->H, cudaMemcpyDeviceToDevice, st));
@@ -853,7 +879,8 @@ struct TmpLevel {
     L.pitch = round_up(w, 32);
     size_t n = (size_t)L.pitch * h;
     size_t fb = (n * 4 + 255) / 256 * 256;
-    if (cudaMalloc(&mem, 3 * fb + n + 256) != cudaSuccess) {
+    size_t bb = (n + 255) / 256 * 256;
+    if (cudaMalloc(&mem, 3 * fb + 2 * bb + 256) != cudaSuccess) {
       cudaGetLastError();
       throw std::bad_alloc();
     }
@@ -861,9 +888,10 @@ struct TmpLevel {
     L.e[0] = (float *)p; p += fb;
     L.e[1] = (float *)p; p += fb;
     L.rhs = (float *)p; p += fb;
-    L.flag = (uint8_t *)p;
+    L.flag = (uint8_t *)p; p += bb;
+    L.code = (uint8_t *)p;
     UBG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    UBG_CUDA(cudaMemsetAsync(mem, 0, 3 * fb + n + 256, st));
+    UBG_CUDA(cudaMemsetAsync(mem, 0, 3 * fb + 2 * bb + 256, st));
   }
   ~TmpLevel() {
     if (st) cudaStreamSynchronize(st);
@@ -875,6 +903,7 @@ struct TmpLevel {
     if (p) UBG_CUDA(cudaMemcpy2DAsync(L.e[0], dp, p, hp, hp, L.h, cudaMemcpyHostToDevice, st));
     UBG_CUDA(cudaMemcpy2DAsync(L.rhs, dp, f, hp, hp, L.h, cudaMemcpyHostToDevice, st));
     upload_flag_u8(L, flag, L.w, L.h, st);
+    level_make_code(L, st);
   }
 };
 }  // namespace

@@ -1,18 +1,18 @@
 // Multigrid pressure solver (class MG, pressure_solver.{hpp,cpp} of
 // te42kyfo/ubootgl) on the GPU.
 //
-//  k_smooth          red-black Gauss-Seidel (rbgs + smoothingKernel,
-//                    pressure_solver.cpp:10-24, 35-89), NS sweeps temporally
-//                    blocked in shared memory; optional prologue that applies
-//                    prolongate + correct (pressure_solver.cpp:134-181) and
-//                    optional zero-gradient boundary after every sweep
-//                    (setZeroGradientBC, pressure_solver.cpp:183-192).
-//  k_resid_restrict  calculateResidualField + restrict fused
-//                    (pressure_solver.cpp:91-132); the fine residual never
-//                    goes to memory.
-//  k_residual        the residual field and its squared L2 norm.
-//  k_coarsen         MG::updateFields (pressure_solver.hpp:34-57), integer
-//                    exact.
+//  k_mg        red-black Gauss-Seidel (rbgs + smoothingKernel,
+//              pressure_solver.cpp:10-24, 35-89), up to 5 sweeps temporally
+//              blocked in shared memory, with an optional prologue
+//              (prolongate + correct, pressure_solver.cpp:134-181), the
+//              zero-gradient boundary after every sweep on level 0
+//              (setZeroGradientBC, pressure_solver.cpp:183-192), and an
+//              optional epilogue that computes the residual and restricts it
+//              to the next level (calculateResidualField + restrict,
+//              pressure_solver.cpp:91-132) without writing the fine residual.
+//  k_mg_tail   the coarse end of the V-cycle in one CTA, in shared memory.
+//  k_residual  the residual field and its squared L2 norm.
+//  k_coarsen   MG::updateFields (pressure_solver.hpp:34-57), integer exact.
 //
 // Red points are those with x+y odd (pressure_solver.cpp:36); a sweep updates
 // all red points, then all black points, which is the reference's
@@ -22,249 +22,423 @@
 
 #include <cstring>
 
+#define ALPHA_IS_ONE(a) ((a) == 1.0f)
+
 namespace ubg {
 namespace {
 
-struct ProlongArgs {
-  const float *ec;       // coarse error (level l+1), null = no prolongation
-  const uint8_t *flagc;  // coarse flag
-  int cpitch;
-  float wsum[5];         // (float)((double)k + 0.0001), k = 0..4
-};
+// Per-cell stencil code of a level: bit 0 = the cell's flag, bits 1..4 = the
+// flags of its west, east, south (y-1) and north (y+1) neighbours (0 on the
+// domain boundary, whose cells are never smoothed).
+constexpr unsigned C_CENTER = 1, C_W = 2, C_E = 4, C_S = 8, C_N = 16;
 
-struct SmoothArgs {
+__global__ void k_make_code(const uint8_t *__restrict__ flag, uint8_t *code, int w, int h,
+                            int P) {
+  int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+  if (x >= w || y >= h) return;
+  size_t i = (size_t)y * P + x;
+  unsigned c = flag[i] ? C_CENTER : 0u;
+  if (x >= 1 && x < w - 1 && y >= 1 && y < h - 1) {
+    if (flag[i - 1]) c |= C_W;
+    if (flag[i + 1]) c |= C_E;
+    if (flag[i - P]) c |= C_S;
+    if (flag[i + P]) c |= C_N;
+  }
+  code[i] = (uint8_t)c;
+}
+
+// smoothingKernel (pressure_solver.cpp:10-24) for alpha = 1.  With flags in
+// {0, 1}, p*flag inside the sum equals flag ? p : 0 (the running sum starts
+// at +0 and never becomes -0), val/sum is exact as a multiplication for
+// sum = 1, 2, 4 and a true division for sum = 3, and flag*val equals
+// flag ? val : 0 up to the sign of a zero.
+__device__ __forceinline__ float rb_update1(unsigned c, float pw, float pe, float ps, float pn,
+                                            float f, float hh) {
+  float val = 0.0f;
+  val = val + ((c & C_W) ? pw : 0.0f);
+  val = val + ((c & C_E) ? pe : 0.0f);
+  val = val + ((c & C_S) ? ps : 0.0f);
+  val = val + ((c & C_N) ? pn : 0.0f);
+  val = val + f * hh * hh;
+  int s = __popc((c >> 1) & 15u);
+  if (s == 3)
+    val = val / 3.0f;
+  else
+    val = val * (s == 4 ? 0.25f : (s == 2 ? 0.5f : (s == 1 ? 1.0f : 0.0f)));
+  if (s == 0) val = 0.0f;
+  return (c & C_CENTER) ? val : 0.0f;
+}
+
+// General alpha (the free function rbgs(p, f, flag, h, alpha)).
+__device__ __forceinline__ float rb_update_alpha(unsigned c, float pc, float pw, float pe,
+                                                 float ps, float pn, float f, float hh,
+                                                 float alpha) {
+  float fw = (c & C_W) ? 1.0f : 0.0f, fe = (c & C_E) ? 1.0f : 0.0f;
+  float fs = (c & C_S) ? 1.0f : 0.0f, fn = (c & C_N) ? 1.0f : 0.0f;
+  float sum = 0.0f;
+  sum = sum + (fw + fe + fn + fs);
+  float val = 0.0f;
+  val = val + pw * fw;
+  val = val + pe * fe;
+  val = val + ps * fs;
+  val = val + pn * fn;
+  val = val + f * hh * hh;
+  val = val / sum;
+  if (sum == 0.0f) val = 0.0f;
+  return ((c & C_CENTER) ? 1.0f : 0.0f) * (alpha * val + (1.0f - alpha) * pc);
+}
+
+// calculateResidualField at one cell (pressure_solver.cpp:100-110): a
+// neighbour term p_n*flag_n + p*(1-flag_n) is flag_n ? p_n : p.
+__device__ __forceinline__ float resid1(unsigned c, float pc, float pw, float pe, float ps,
+                                        float pn, float f, float ihsq) {
+  float val = 0.0f;
+  val = val + ((c & C_W) ? pw : pc);
+  val = val + ((c & C_E) ? pe : pc);
+  val = val + ((c & C_S) ? ps : pc);
+  val = val + ((c & C_N) ? pn : pc);
+  val = val + -4.0f * pc;
+  val = val * ihsq;
+  return (c & C_CENTER) ? (f + val) : 0.0f;
+}
+
+struct MgArgs {
   const float *in;
   float *out;
   const float *rhs;
-  const uint8_t *flag;
+  const uint8_t *code;
   int w, h, pitch;
-  float hh;
-  float alpha;
-  int nsweeps;
-  int zgbc;
-  int zero_init;
-  ProlongArgs pr;
+  float hh, alpha, ihsq;
+  int nsweeps, zgbc, zero_init;
+  // prologue: p += prolongate(ec) (post-smoothing)
+  const float *ec;
+  const uint8_t *codec;
+  int cpitch;
+  float wsum[5];  // (float)((double)k + 0.0001)
+  // epilogue: rc = restrict(residual) (pre-smoothing)
+  float *rc;
+  int cw, ch;
+  // epilogue: sum of r^2 over the tile's interior cells
+  double *norm2;
 };
 
-template <int TX, int TY, int HALO>
-struct SmoothTile {
-  static constexpr int RX = TX + 2 * HALO;
-  static constexpr int RY = TY + 2 * HALO;
-  static constexpr size_t smem() { return (size_t)RX * RY * (4 + 4 + 1); }
-};
-
-// prolongate (pressure_solver.cpp:134-172) evaluated at one fine cell.
-__device__ __forceinline__ float prolong_at(const ProlongArgs &pr, int gx, int gy, int w, int h,
-                                            float fine) {
+// prolongate (pressure_solver.cpp:134-172) at one fine interior cell whose
+// own flag is set.
+__device__ __forceinline__ float prolong_at(const MgArgs &a, int gx, int gy) {
   int cx = gx >> 1, cy = gy >> 1;
-  const float *ec = pr.ec;
-  const uint8_t *fc = pr.flagc;
-  int cp = pr.cpitch;
+  const float *ec = a.ec;
+  const uint8_t *fc = a.codec;
+  int cp = a.cpitch;
   auto E = [&](int x, int y) { return __ldg(ec + (size_t)y * cp + x); };
-  auto F = [&](int x, int y) { return (int)__ldg(fc + (size_t)y * cp + x); };
+  auto F = [&](int x, int y) { return (int)(__ldg(fc + (size_t)y * cp + x) & 1u); };
   bool xo = gx & 1, yo = gy & 1;
-  if (!xo && !yo) return E(cx, cy) * fine;
+  if (!xo && !yo) return E(cx, cy);
   if (xo && !yo) {
-    if (gx >= w - 2) return 0.0f;
-    float sum = pr.wsum[F(cx, cy) + F(cx + 1, cy)];
-    return fine * (E(cx, cy) + E(cx + 1, cy)) / sum;
+    if (gx >= a.w - 2) return 0.0f;
+    float sum = a.wsum[F(cx, cy) + F(cx + 1, cy)];
+    return (E(cx, cy) + E(cx + 1, cy)) / sum;
   }
   if (!xo && yo) {
-    if (gy >= h - 2) return 0.0f;
-    float sum = pr.wsum[F(cx, cy) + F(cx, cy + 1)];
-    return fine * (E(cx, cy) + E(cx, cy + 1)) / sum;
+    if (gy >= a.h - 2) return 0.0f;
+    float sum = a.wsum[F(cx, cy) + F(cx, cy + 1)];
+    return (E(cx, cy) + E(cx, cy + 1)) / sum;
   }
-  if (gx >= w - 2 || gy >= h - 2) return 0.0f;
-  float sum = pr.wsum[F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1)];
-  return fine * (((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1)) / sum;
+  if (gx >= a.w - 2 || gy >= a.h - 2) return 0.0f;
+  float sum = a.wsum[F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1)];
+  return (((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1)) / sum;
 }
 
 template <int TX, int TY, int HALO>
-__global__ void __launch_bounds__(256) k_smooth(SmoothArgs a) {
-  using T = SmoothTile<TX, TY, HALO>;
-  constexpr int RX = T::RX, RY = T::RY;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *sp = reinterpret_cast<float *>(smem_raw);
-  float *sf = sp + RX * RY;
-  uint8_t *sfl = reinterpret_cast<uint8_t *>(sf + RX * RY);
+struct Tile {
+  static constexpr int RX = TX + 2 * HALO, RY = TY + 2 * HALO, HX = RX / 2;
+  // coarse window for the prolongation prologue
+  static constexpr int CW = HX + 2, CH = RY / 2 + 2;
+  static_assert(RX % 4 == 0 && HALO % 4 == 0 && TX % 4 == 0 && TY % 2 == 0, "tile alignment");
+  static constexpr size_t smem() {
+    return (size_t)2 * RY * HX * (4 + 4 + 1) + (size_t)CW * CH * 4 + ((size_t)CW * CH + 15) / 16 * 16;
+  }
+};
 
-  const int tid = threadIdx.x, nt = blockDim.x;
+// One multigrid smoothing launch on a tile of TX x TY cells with a halo of
+// HALO cells, all in shared memory in a red/black-split layout: cell (rx, ry)
+// of the region lives in colour array (rx+ry)&1 at [ry][rx/2], so the four
+// neighbours of a cell are consecutive entries of the other colour's rows
+// (no bank conflicts).  Red = (x+y) odd; region parity equals global parity
+// because x0 + y0 is even.  After half sweep i only cells within HALO - i of
+// the tile are still exact, so each half sweep updates just that cone.
+template <int TX, int TY, int HALO, bool ALPHA1, int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 6) k_mg(MgArgs a) {
+  constexpr int NTY = NT / 32;
+  using T = Tile<TX, TY, HALO>;
+  constexpr int RX = T::RX, RY = T::RY, HX = T::HX;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *sp = reinterpret_cast<float *>(smem_raw);  // [2][RY][HX]
+  float *sf = sp + 2 * RY * HX;
+  uint8_t *sc = reinterpret_cast<uint8_t *>(sf + 2 * RY * HX);
+  auto IDX = [](int rx, int ry) { return (((rx + ry) & 1) * RY + ry) * HX + (rx >> 1); };
+
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
   const int x0 = blockIdx.x * TX - HALO, y0 = blockIdx.y * TY - HALO;
   const int w = a.w, h = a.h, P = a.pitch;
 
-  for (int i = tid; i < RX * RY; i += nt) {
-    int ry = i / RX, rx = i - ry * RX;
-    int gx = x0 + rx, gy = y0 + ry;
-    bool in = gx >= 0 && gx < w && gy >= 0 && gy < h;
-    size_t gi = (size_t)gy * P + gx;
-    float pv = 0.0f, fv = 0.0f;
-    uint8_t flv = 0;
-    if (in) {
-      if (!a.zero_init) pv = __ldg(a.in + gi);
-      fv = __ldg(a.rhs + gi);
-      flv = __ldg(a.flag + gi);
+  // ---- load p, f, code (float4 / uchar4 per thread; x0 is a multiple of 4);
+  // all of a thread's loads are issued before the first shared-memory store
+  constexpr int NQ = RY * (RX / 4), NIT = (NQ + NT - 1) / NT;
+  float4 pv[NIT], fv[NIT];
+  uchar4 cv[NIT];
+#pragma unroll
+  for (int it = 0; it < NIT; it++) {
+    int q = tid + it * NT;
+    int ry = q / (RX / 4), g = q - ry * (RX / 4);
+    int gx = x0 + 4 * g, gy = y0 + ry;
+    pv[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+    fv[it] = pv[it];
+    cv[it] = make_uchar4(0, 0, 0, 0);
+    if (q < NQ && gy >= 0 && gy < h && gx >= 0 && gx < w) {
+      size_t gi = (size_t)gy * P + gx;
+      if (!a.zero_init) pv[it] = __ldg(reinterpret_cast<const float4 *>(a.in + gi));
+      fv[it] = __ldg(reinterpret_cast<const float4 *>(a.rhs + gi));
+      cv[it] = __ldg(reinterpret_cast<const uchar4 *>(a.code + gi));
     }
-    if (a.pr.ec && in && gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1)
-      pv = pv + prolong_at(a.pr, gx, gy, w, h, (float)flv);
-    sp[i] = pv;
-    sf[i] = fv;
-    sfl[i] = flv;
+  }
+#pragma unroll
+  for (int it = 0; it < NIT; it++) {
+    int q = tid + it * NT;
+    if (q >= NQ) break;
+    int ry = q / (RX / 4), g = q - ry * (RX / 4);
+    int gx = x0 + 4 * g;
+    float4 p4 = pv[it], f4 = fv[it];
+    uchar4 c4 = cv[it];
+    if (gx + 3 >= w) {
+      if (gx + 1 >= w) { p4.y = 0.f; f4.y = 0.f; c4.y = 0; }
+      if (gx + 2 >= w) { p4.z = 0.f; f4.z = 0.f; c4.z = 0; }
+      p4.w = 0.f; f4.w = 0.f; c4.w = 0;
+    }
+    int c0 = ry & 1;
+    int base0 = (c0 * RY + ry) * HX + 2 * g, base1 = ((c0 ^ 1) * RY + ry) * HX + 2 * g;
+    *reinterpret_cast<float2 *>(sp + base0) = make_float2(p4.x, p4.z);
+    *reinterpret_cast<float2 *>(sp + base1) = make_float2(p4.y, p4.w);
+    *reinterpret_cast<float2 *>(sf + base0) = make_float2(f4.x, f4.z);
+    *reinterpret_cast<float2 *>(sf + base1) = make_float2(f4.y, f4.w);
+    sc[base0] = c4.x;
+    sc[base0 + 1] = c4.z;
+    sc[base1] = c4.y;
+    sc[base1 + 1] = c4.w;
   }
   __syncthreads();
 
-  auto zero_gradient = [&]() {
-    // setZeroGradientBC on the cells of this region (corners untouched).
-    for (int i = tid; i < RX * RY; i += nt) {
-      int ry = i / RX, rx = i - ry * RX;
-      int gx = x0 + rx, gy = y0 + ry;
-      if (gy >= 1 && gy < h - 1) {
-        if (gx == 0 && rx + 1 < RX) sp[i] = sp[i + 1];
-        if (gx == w - 1 && rx >= 1) sp[i] = sp[i - 1];
+  // ---- prologue: correct(p, prolongate(ec)) on the interior cells, with
+  // the coarse window staged in shared memory
+  if (a.ec) {
+    constexpr int CW = T::CW, CH = T::CH;
+    float *sec = reinterpret_cast<float *>(sc + 2 * RY * HX);
+    uint8_t *scf = reinterpret_cast<uint8_t *>(sec + CW * CH);
+    const int cxa = x0 >> 1, cya = y0 >> 1;
+    for (int q = tid; q < CW * CH; q += NT) {
+      int ly = q / CW, lx = q - ly * CW;
+      int cx = cxa + lx, cy = cya + ly;
+      float e = 0.0f;
+      uint8_t fc = 0;
+      if (cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
+        e = __ldg(a.ec + (size_t)cy * a.cpitch + cx);
+        fc = __ldg(a.codec + (size_t)cy * a.cpitch + cx) & 1u;
       }
-      if (gx >= 1 && gx < w - 1) {
-        if (gy == 0 && ry + 1 < RY) sp[i] = sp[i + RX];
-        if (gy == h - 1 && ry >= 1) sp[i] = sp[i - RX];
+      sec[q] = e;
+      scf[q] = fc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int color = 0; color < 2; color++) {
+      for (int ry = ty; ry < RY; ry += NTY) {
+        const int par = (ry + color) & 1;
+        const int gy = y0 + ry;
+        if (gy < 1 || gy >= h - 1) continue;
+        for (int k = tx; k < HX; k += 32) {
+          int rx = 2 * k + par, gx = x0 + rx;
+          int i = (color * RY + ry) * HX + k;
+          if (gx < 1 || gx >= w - 1 || !(sc[i] & C_CENTER)) continue;
+          // prolongate (pressure_solver.cpp:134-172); e * fine flag = e here
+          const float *E = sec + (ry >> 1) * CW + (rx >> 1);
+          const uint8_t *F = scf + (ry >> 1) * CW + (rx >> 1);
+          bool xo = gx & 1, yo = gy & 1;
+          float ev;
+          if (!xo && !yo) {
+            ev = E[0];
+          } else if (xo && !yo) {
+            ev = (gx >= w - 2) ? 0.0f : (E[0] + E[1]) / a.wsum[F[0] + F[1]];
+          } else if (!xo && yo) {
+            ev = (gy >= h - 2) ? 0.0f : (E[0] + E[CW]) / a.wsum[F[0] + F[CW]];
+          } else {
+            ev = (gx >= w - 2 || gy >= h - 2)
+                     ? 0.0f
+                     : (((E[0] + E[CW + 1]) + E[1]) + E[CW]) / a.wsum[F[0] + F[CW + 1] + F[1] + F[CW]];
+          }
+          sp[i] = sp[i] + ev;
+        }
       }
     }
+    __syncthreads();
+  }
+
+  // setZeroGradientBC on this region (only tiles that touch the domain edge)
+  const bool edge = x0 <= 0 || y0 <= 0 || x0 + RX >= w || y0 + RY >= h;
+  auto zero_gradient = [&]() {
+    for (int q = tid; q < 2 * RY; q += NT) {
+      int ry = q >> 1, side = q & 1;
+      int gy = y0 + ry;
+      if (gy < 1 || gy >= h - 1) continue;
+      int rx = side ? (w - 1 - x0) : (0 - x0);
+      int rn = side ? rx - 1 : rx + 1;
+      if (rx < 0 || rx >= RX || rn < 0 || rn >= RX) continue;
+      sp[IDX(rx, ry)] = sp[IDX(rn, ry)];
+    }
+    for (int q = tid; q < 2 * RX; q += NT) {
+      int rx = q >> 1, side = q & 1;
+      int gx = x0 + rx;
+      if (gx < 1 || gx >= w - 1) continue;
+      int ry = side ? (h - 1 - y0) : (0 - y0);
+      int rn = side ? ry - 1 : ry + 1;
+      if (ry < 0 || ry >= RY || rn < 0 || rn >= RY) continue;
+      sp[IDX(rx, ry)] = sp[IDX(rx, rn)];
+    }
   };
-  if (a.zgbc && a.pr.ec) {
+  if (a.zgbc && edge && a.ec) {
     zero_gradient();
     __syncthreads();
   }
 
-  const float hh = a.hh, alpha = a.alpha;
-  constexpr int HALFW = (RX - 2) / 2;
-  constexpr int NCELL = (RY - 2) * HALFW;
+  // ---- red-black sweeps
+  const float hh = a.hh;
+  const bool inner = x0 >= 1 && y0 >= 1 && x0 + RX <= w - 1 && y0 + RY <= h - 1;
+  int half = 0;
   for (int s = 0; s < a.nsweeps; s++) {
 #pragma unroll
-    for (int color = 1; color >= 0; color--) {  // red (x+y odd) first, then black
-      for (int k = tid; k < NCELL; k += nt) {
-        int ry = 1 + k / HALFW;
-        int j = k - (ry - 1) * HALFW;
-        int off = color ? (ry & 1) : ((ry + 1) & 1);
-        int rx = 1 + 2 * j + off;
-        int gx = x0 + rx, gy = y0 + ry;
-        if (gx < 1 || gx >= w - 1 || gy < 1 || gy >= h - 1) continue;
-        int i = ry * RX + rx;
-        float fw = (float)sfl[i - 1], fe = (float)sfl[i + 1];
-        float fs = (float)sfl[i - RX], fn = (float)sfl[i + RX];
-        float sum = 0.0f;
-        sum = sum + (fw + fe + fn + fs);
-        float val = 0.0f;
-        val = val + sp[i - 1] * fw;
-        val = val + sp[i + 1] * fe;
-        val = val + sp[i - RX] * fs;
-        val = val + sp[i + RX] * fn;
-        val = val + sf[i] * hh * hh;
-        val = val / sum;
-        if (sum == 0.0f) val = 0.0f;
-        sp[i] = (float)sfl[i] * (alpha * val + (1.0f - alpha) * sp[i]);
+    for (int color = 1; color >= 0; color--) {
+      half++;
+      float *self = sp + color * RY * HX;
+      const float *oth = sp + (color ^ 1) * RY * HX;
+      const float *fs = sf + color * RY * HX;
+      const uint8_t *cs = sc + color * RY * HX;
+      for (int ry = half + ty; ry <= RY - 1 - half; ry += NTY) {
+        const int par = (ry + color) & 1;
+        const int gy = y0 + ry;
+#pragma unroll
+        for (int kk = 0; kk < (HX + 31) / 32; kk++) {
+          const int k = kk * 32 + tx;
+          // all of a row is exact enough to compute (the cone is cut by rows
+          // only); the two end cells lack a neighbour in the region
+          bool ok = k >= 1 - par && k <= HX - 1 - par;
+          if (!inner) {
+            int gx = x0 + 2 * k + par;
+            ok = ok && gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1;
+          }
+          if (!ok) continue;
+          const int i = ry * HX + k;
+          const unsigned c = cs[i];
+          const float pw = oth[i - 1 + par], pe = oth[i + par];
+          const float ps = oth[i - HX], pn = oth[i + HX];
+          const float f = fs[i];
+          float v;
+          if (ALPHA1) {
+            if (c == (C_CENTER | C_W | C_E | C_S | C_N))
+              v = ((((pw + pe) + ps) + pn) + f * hh * hh) * 0.25f;
+            else
+              v = rb_update1(c, pw, pe, ps, pn, f, hh);
+          } else {
+            v = rb_update_alpha(c, self[i], pw, pe, ps, pn, f, hh, a.alpha);
+          }
+          self[i] = v;
+        }
       }
       __syncthreads();
     }
-    if (a.zgbc) {
+    if (a.zgbc && edge) {
       zero_gradient();
       __syncthreads();
     }
   }
 
-  for (int i = tid; i < TX * TY; i += nt) {
-    int ty = i / TX, tx = i - ty * TX;
-    int gx = x0 + HALO + tx, gy = y0 + HALO + ty;
-    if (gx < w && gy < h) a.out[(size_t)gy * P + gx] = sp[(ty + HALO) * RX + tx + HALO];
+  // ---- write the tile (float4; gx is a multiple of 4)
+  for (int q = tid; q < TY * (TX / 4); q += NT) {
+    int ty2 = q / (TX / 4), g = q - ty2 * (TX / 4);
+    int ry = HALO + ty2, rx = HALO + 4 * g;
+    int gx = x0 + rx, gy = y0 + ry;
+    if (gy >= h || gx >= w) continue;
+    int c0 = (rx + ry) & 1;
+    int b0 = (c0 * RY + ry) * HX + (rx >> 1), b1 = ((c0 ^ 1) * RY + ry) * HX + (rx >> 1);
+    float2 u = *reinterpret_cast<const float2 *>(sp + b0);
+    float2 v = *reinterpret_cast<const float2 *>(sp + b1);
+    float4 o = make_float4(u.x, v.x, u.y, v.y);
+    float *dst = a.out + (size_t)gy * P + gx;
+    if (gx + 3 < w) {
+      *reinterpret_cast<float4 *>(dst) = o;
+    } else {
+      dst[0] = o.x;
+      if (gx + 1 < w) dst[1] = o.y;
+      if (gx + 2 < w) dst[2] = o.z;
+    }
   }
-}
 
-// ---------------------------------------------------- residual + restrict
-struct RRArgs {
-  const float *p, *rhs;
-  const uint8_t *flag;
-  int w, h, pitch;
-  float ihsq;
-  float *rc;      // coarse output
-  int cw, ch, cpitch;
-  double *norm2;  // optional: sum of r^2 over the fine interior
-};
-
-constexpr int CTX = 32, CTY = 8;
-
-__device__ __forceinline__ float residual_at(const float *sp, const uint8_t *sfl, int i, int RX,
-                                             float f, float ihsq) {
-  float pc = sp[i];
-  float fw = (float)sfl[i - 1], fe = (float)sfl[i + 1];
-  float fs = (float)sfl[i - RX], fn = (float)sfl[i + RX];
-  float val = 0.0f;
-  val = val + (sp[i - 1] * fw + pc * (1.0f - fw));
-  val = val + (sp[i + 1] * fe + pc * (1.0f - fe));
-  val = val + (sp[i - RX] * fs + pc * (1.0f - fs));
-  val = val + (sp[i + RX] * fn + pc * (1.0f - fn));
-  val = val + -4.0f * pc;
-  val = val * ihsq;
-  return (f + val) * (float)sfl[i];
-}
-
-__device__ __forceinline__ void block_add_double(double v, double *out) {
-  if (!out) return;
-  __shared__ double red[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) red[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    int nw = blockDim.x >> 5;
-    v = lane < nw ? red[lane] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) atomicAdd(out, v);
-  }
-}
-
-__global__ void __launch_bounds__(256) k_resid_restrict(RRArgs a) {
-  constexpr int PRX = 2 * CTX + 3, PRY = 2 * CTY + 3;  // p / flag region
-  constexpr int RRX = 2 * CTX + 1, RRY = 2 * CTY + 1;  // residual region
-  __shared__ float sp[PRY * PRX];
-  __shared__ uint8_t sfl[PRY * PRX];
-  __shared__ float sr[RRY * RRX];
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int X0 = blockIdx.x * CTX, Y0 = blockIdx.y * CTY;
-  const int px0 = 2 * X0 - 2, py0 = 2 * Y0 - 2;
-  const int w = a.w, h = a.h, P = a.pitch;
-  for (int i = tid; i < PRX * PRY; i += nt) {
-    int ry = i / PRX, rx = i - ry * PRX;
-    int gx = px0 + rx, gy = py0 + ry;
-    bool in = gx >= 0 && gx < w && gy >= 0 && gy < h;
-    sp[i] = in ? __ldg(a.p + (size_t)gy * P + gx) : 0.0f;
-    sfl[i] = in ? __ldg(a.flag + (size_t)gy * P + gx) : (uint8_t)0;
-  }
-  __syncthreads();
+  if (!a.rc && !a.norm2) return;
+  // ---- residual on the tile grown by one cell (in place into f) ----------
   double acc = 0.0;
-  for (int i = tid; i < RRX * RRY; i += nt) {
-    int j = i / RRX, k = i - j * RRX;
-    int gx = px0 + 1 + k, gy = py0 + 1 + j;
-    float r = 0.0f;
-    if (gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1) {
-      float f = __ldg(a.rhs + (size_t)gy * P + gx);
-      r = residual_at(sp, sfl, (j + 1) * PRX + (k + 1), PRX, f, a.ihsq);
-      if (a.norm2 && gx >= 2 * X0 && gx < 2 * (X0 + CTX) && gy >= 2 * Y0 && gy < 2 * (Y0 + CTY))
-        acc += (double)r * (double)r;
+  const int rlo = a.rc ? HALO - 1 : HALO;
+  const int rhix = a.rc ? HALO + TX : HALO + TX - 1, rhiy = a.rc ? HALO + TY : HALO + TY - 1;
+#pragma unroll
+  for (int color = 0; color < 2; color++) {
+    const float *self = sp + color * RY * HX;
+    const float *oth = sp + (color ^ 1) * RY * HX;
+    float *fs = sf + color * RY * HX;
+    const uint8_t *cs = sc + color * RY * HX;
+    for (int ry = rlo + ty; ry <= rhiy; ry += NTY) {
+      const int par = (ry + color) & 1;
+      const int gy = y0 + ry;
+      for (int k = tx; k < HX; k += 32) {
+        const int rx = 2 * k + par, gx = x0 + rx;
+        if (rx < rlo || rx > rhix) continue;
+        const int i = ry * HX + k;
+        float r = 0.0f;
+        if (gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1) {
+          r = resid1(cs[i], self[i], oth[i - 1 + par], oth[i + par], oth[i - HX], oth[i + HX], fs[i],
+                     a.ihsq);
+          if (a.norm2 && rx >= HALO && rx < HALO + TX && ry >= HALO && ry < HALO + TY)
+            acc += (double)r * (double)r;
+        }
+        if (a.rc) fs[i] = r;
+      }
     }
-    sr[i] = r;
   }
   __syncthreads();
-  for (int i = tid; i < CTX * CTY; i += nt) {
-    int ty = i / CTX, tx = i - ty * CTX;
-    int X = X0 + tx, Y = Y0 + ty;
-    if (X >= a.cw || Y >= a.ch) continue;
-    float v = 0.0f;
-    if (X >= 1 && X < a.cw - 1 && Y >= 1 && Y < a.ch - 1) {
-      const float *c = sr + (2 * ty + 1) * RRX + (2 * tx + 1);
-      v = (c[-RRX - 1] * 1.0f + c[-RRX] * 2.0f) + c[-RRX + 1] * 1.0f;
-      v = v + ((c[-1] * 2.0f + c[0] * 4.0f) + c[1] * 2.0f);
-      v = v + ((c[RRX - 1] * 1.0f + c[RRX] * 2.0f) + c[RRX + 1] * 1.0f);
-      v = v * (1.0f / 16.0f);
+  if (a.norm2) {
+    __shared__ double red[NTY];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (tx == 0) red[ty] = acc;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int i = 0; i < NTY; i++) t += red[i];
+      atomicAdd(a.norm2, t);
     }
-    a.rc[(size_t)Y * a.cpitch + X] = v;
   }
-  block_add_double(acc, a.norm2);
+  // ---- restrict (pressure_solver.cpp:118-132) onto the coarse tile -------
+  if (a.rc) {
+    const int cx0 = blockIdx.x * (TX / 2), cy0 = blockIdx.y * (TY / 2);
+    for (int q = tid; q < (TX / 2) * (TY / 2); q += NT) {
+      int cyy = q / (TX / 2), cxx = q - cyy * (TX / 2);
+      int X = cx0 + cxx, Y = cy0 + cyy;
+      if (X >= a.cw || Y >= a.ch) continue;
+      float v = 0.0f;
+      if (X >= 1 && X < a.cw - 1 && Y >= 1 && Y < a.ch - 1) {
+        int rx = 2 * X - x0, ry = 2 * Y - y0;
+        auto R = [&](int dx, int dy) { return sf[IDX(rx + dx, ry + dy)]; };
+        v = (R(-1, -1) * 1.0f + R(0, -1) * 2.0f) + R(1, -1) * 1.0f;
+        v = v + ((R(-1, 0) * 2.0f + R(0, 0) * 4.0f) + R(1, 0) * 2.0f);
+        v = v + ((R(-1, 1) * 1.0f + R(0, 1) * 2.0f) + R(1, 1) * 1.0f);
+        v = v * (1.0f / 16.0f);
+      }
+      a.rc[(size_t)Y * a.cpitch + X] = v;
+    }
+  }
 }
 
 // ------------------------------------------------------ residual field only
@@ -326,84 +500,242 @@ __global__ void k_fill_u8(uint8_t *p, int w, int h, int pitch, uint8_t v) {
   if (x < w && y < h) p[(size_t)y * pitch + x] = v;
 }
 
-// ---------------------------------------------------------------- helpers
-template <int TX, int TY, int HALO>
-void launch_smooth_t(const SmoothArgs &a, cudaStream_t st) {
-  using T = SmoothTile<TX, TY, HALO>;
-  static_assert(T::smem() <= 48 * 1024, "smoother tile exceeds the default shared-memory limit");
-  size_t sm = T::smem();
+// ------------------------------------------------------------ tail solver
+// The coarse end of the V-cycle (levels lt .. levels-2) in one launch of one
+// 1024-thread CTA, every level resident in shared memory: down (zero initial
+// guess, 3 sweeps, residual, restrict), 5 sweeps on the coarsest level, up
+// (prolongate + correct, 3 sweeps).  Same arithmetic as the tiled kernels.
+constexpr int TAIL_MAXL = 12;
+constexpr int TAIL_THREADS = 1024;
+constexpr size_t TAIL_SMEM_MAX = 160 * 1024;
+
+struct TailLevel {
+  int w, h;
+  float hh, ihsq;
+  int oe, orr, orhs, oc;  // offsets: floats for e / r / rhs, bytes for code
+};
+struct TailArgs {
+  int nlev;
+  TailLevel L[TAIL_MAXL];
+  const uint8_t *code[TAIL_MAXL];
+  int code_pitch[TAIL_MAXL];
+  const float *rhs_top;
+  int rhs_pitch;
+  float *e_top;
+  int e_pitch;
+  int float_words;  // size of the float part of shared memory
+  float wsum[5];
+};
+
+__global__ void __launch_bounds__(TAIL_THREADS) k_mg_tail(TailArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *fm = reinterpret_cast<float *>(smem_raw);
+  uint8_t *bm = smem_raw + (size_t)a.float_words * 4;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+  const int nl = a.nlev;
+
+  for (int t = 0; t < nl; t++) {
+    const TailLevel &L = a.L[t];
+    for (int q = tid; q < L.w * L.h; q += TAIL_THREADS) {
+      int y = q / L.w, x = q - y * L.w;
+      bm[L.oc + q] = a.code[t][(size_t)y * a.code_pitch[t] + x];
+      fm[L.oe + q] = 0.0f;
+      if (t == 0) fm[L.orhs + q] = a.rhs_top[(size_t)y * a.rhs_pitch + x];
+    }
+  }
+  __syncthreads();
+
+  auto sweeps = [&](int t, int ns) {
+    const TailLevel &L = a.L[t];
+    float *e = fm + L.oe;
+    const float *f = fm + L.orhs;
+    const uint8_t *c = bm + L.oc;
+    const int w = L.w, hw2 = (w + 1) / 2;
+    for (int s = 0; s < ns; s++) {
+      for (int color = 1; color >= 0; color--) {
+        for (int y = 1 + ty; y < L.h - 1; y += 32) {
+          int par = (y + color) & 1;
+          for (int j = tx; j < hw2; j += 32) {
+            int x = 2 * j + par;
+            if (x < 1 || x >= w - 1) continue;
+            int i = y * w + x;
+            e[i] = rb_update1(c[i], e[i - 1], e[i + 1], e[i - w], e[i + w], f[i], L.hh);
+          }
+        }
+        __syncthreads();
+      }
+    }
+  };
+
+  // down
+  for (int t = 0; t < nl; t++) {
+    if (t == nl - 1) {
+      sweeps(t, 5);
+      break;
+    }
+    sweeps(t, 3);
+    const TailLevel &L = a.L[t], &C = a.L[t + 1];
+    float *e = fm + L.oe, *r = fm + L.orr;
+    const float *f = fm + L.orhs;
+    const uint8_t *c = bm + L.oc;
+    for (int q = tid; q < L.w * L.h; q += TAIL_THREADS) {
+      int y = q / L.w, x = q - y * L.w;
+      float rv = 0.0f;
+      if (x >= 1 && x < L.w - 1 && y >= 1 && y < L.h - 1)
+        rv = resid1(c[q], e[q], e[q - 1], e[q + 1], e[q - L.w], e[q + L.w], f[q], L.ihsq);
+      r[q] = rv;
+    }
+    __syncthreads();
+    float *rc = fm + C.orhs;
+    for (int q = tid; q < C.w * C.h; q += TAIL_THREADS) {
+      int Y = q / C.w, X = q - Y * C.w;
+      float v = 0.0f;
+      if (X >= 1 && X < C.w - 1 && Y >= 1 && Y < C.h - 1) {
+        const float *R0 = r + (2 * Y) * L.w + 2 * X;
+        v = (R0[-L.w - 1] * 1.0f + R0[-L.w] * 2.0f) + R0[-L.w + 1] * 1.0f;
+        v = v + ((R0[-1] * 2.0f + R0[0] * 4.0f) + R0[1] * 2.0f);
+        v = v + ((R0[L.w - 1] * 1.0f + R0[L.w] * 2.0f) + R0[L.w + 1] * 1.0f);
+        v = v * (1.0f / 16.0f);
+      }
+      rc[q] = v;
+    }
+    __syncthreads();
+  }
+  // up
+  for (int t = nl - 2; t >= 0; t--) {
+    const TailLevel &L = a.L[t], &C = a.L[t + 1];
+    float *e = fm + L.oe;
+    const float *ec = fm + C.oe;
+    const uint8_t *c = bm + L.oc, *cc = bm + C.oc;
+    for (int q = tid; q < L.w * L.h; q += TAIL_THREADS) {
+      int y = q / L.w, x = q - y * L.w;
+      if (x < 1 || x >= L.w - 1 || y < 1 || y >= L.h - 1 || !(c[q] & C_CENTER)) continue;
+      int cx = x >> 1, cy = y >> 1;
+      auto E = [&](int xx, int yy) { return ec[yy * C.w + xx]; };
+      auto F = [&](int xx, int yy) { return (int)(cc[yy * C.w + xx] & 1u); };
+      bool xo = x & 1, yo = y & 1;
+      float ev;
+      if (!xo && !yo)
+        ev = E(cx, cy);
+      else if (xo && !yo)
+        ev = (x >= L.w - 2) ? 0.0f : (E(cx, cy) + E(cx + 1, cy)) / a.wsum[F(cx, cy) + F(cx + 1, cy)];
+      else if (!xo && yo)
+        ev = (y >= L.h - 2) ? 0.0f : (E(cx, cy) + E(cx, cy + 1)) / a.wsum[F(cx, cy) + F(cx, cy + 1)];
+      else
+        ev = (x >= L.w - 2 || y >= L.h - 2)
+                 ? 0.0f
+                 : (((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1)) /
+                       a.wsum[F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1)];
+      e[q] = e[q] + ev;
+    }
+    __syncthreads();
+    sweeps(t, 3);
+  }
+  const TailLevel &L0 = a.L[0];
+  for (int q = tid; q < L0.w * L0.h; q += TAIL_THREADS) {
+    int y = q / L0.w, x = q - y * L0.w;
+    a.e_top[(size_t)y * a.e_pitch + x] = fm[L0.oe + q];
+  }
+}
+
+
+// ------------------------------------------------------------ launches
+template <int TX, int TY, int HALO, bool A1, int NT = 256>
+void launch_mg_t(const MgArgs &a, cudaStream_t st) {
+  using T = Tile<TX, TY, HALO>;
   dim3 grid((a.w + TX - 1) / TX, (a.h + TY - 1) / TY);
-  k_smooth<TX, TY, HALO><<<grid, 256, sm, st>>>(a);
+  k_mg<TX, TY, HALO, A1, NT><<<grid, dim3(32, NT / 32), T::smem(), st>>>(a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
 
-// Halo of a temporally blocked tile: each red-black sweep needs two cells,
-// plus one so that the zero-gradient copy of a tile whose first column is
-// the domain's last column (p(w-1, y) = p(w-2, y)) reads a valid neighbour.
-// x0 + y0 stays even, so region parity equals global parity.
-void launch_smooth(const SmoothArgs &a, cudaStream_t st) {
-  switch (a.nsweeps) {
-    case 1: launch_smooth_t<64, 32, 3>(a, st); break;
-    case 2: launch_smooth_t<64, 32, 5>(a, st); break;
-    case 3: launch_smooth_t<64, 32, 7>(a, st); break;
-    case 4: launch_smooth_t<64, 32, 9>(a, st); break;
-    case 5: launch_smooth_t<64, 32, 11>(a, st); break;
-    default: throw ArgError("smoother: 1..5 sweeps per launch");
+template <int TX, int TY, int HALO, bool A1, int NT = 256>
+void set_smem_attr() {
+  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)Tile<TX, TY, HALO>::smem()));
+}
+
+void init_kernel_attributes() {
+  static bool done = false;
+  if (done) return;
+  set_smem_attr<112, 32, 8, true, 512>();
+  set_smem_attr<48, 16, 8, true>();
+  set_smem_attr<40, 8, 12, true>();
+  set_smem_attr<56, 24, 4, false>();
+  UBG_CUDA(cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TAIL_SMEM_MAX));
+  done = true;
+}
+
+// 3 sweeps with an optional restriction epilogue need HALO >= 8; the tile
+// is chosen by level width so small levels still fill the GPU.
+void launch_mg(const MgArgs &a, cudaStream_t st) {
+  if (!ALPHA_IS_ONE(a.alpha) || a.nsweeps == 1) {
+    if (a.nsweeps != 1) throw ArgError("general alpha: one sweep per launch");
+    launch_mg_t<56, 24, 4, false>(a, st);
+  } else if (a.nsweeps <= 3) {
+    if (a.w >= 448)
+      launch_mg_t<112, 32, 8, true, 512>(a, st);
+    else
+      launch_mg_t<48, 16, 8, true>(a, st);
+  } else if (a.nsweeps <= 5) {
+    launch_mg_t<40, 8, 12, true>(a, st);
+  } else {
+    throw ArgError("smoother: at most 5 sweeps per launch");
   }
 }
 
-ProlongArgs make_prolong(const MgLevel *coarse, int cur) {
-  ProlongArgs pr{};
-  if (!coarse) return pr;
-  pr.ec = coarse->e[cur];
-  pr.flagc = coarse->flag;
-  pr.cpitch = coarse->pitch;
-  for (int k = 0; k < 5; k++) pr.wsum[k] = (float)((double)(float)k + 0.0001);
-  return pr;
-}
-
-void smooth(MgHier &mg, std::vector<int> &cur, int l, int ns, bool zgbc, bool zero_init,
-            const MgLevel *prolong_from, int prolong_cur, float alpha, cudaStream_t st) {
-  MgLevel &L = mg.lv[l];
-  ProfScope ps_(l == 0 ? KC_SMOOTH_L0 : KC_SMOOTH_COARSE, st);
-  SmoothArgs a{};
-  a.in = L.e[cur[l]];
-  a.out = L.e[1 - cur[l]];
+MgArgs level_args(MgLevel &L, const float *in, float *out, int ns, float alpha) {
+  MgArgs a{};
+  a.in = in;
+  a.out = out;
   a.rhs = L.rhs;
-  a.flag = L.flag;
+  a.code = L.code;
   a.w = L.w;
   a.h = L.h;
   a.pitch = L.pitch;
   a.hh = L.hh;
   a.alpha = alpha;
+  a.ihsq = 1.0f / L.hh / L.hh;
   a.nsweeps = ns;
-  a.zgbc = zgbc ? 1 : 0;
-  a.zero_init = zero_init ? 1 : 0;
-  a.pr = make_prolong(prolong_from, prolong_cur);
-  launch_smooth(a, st);
-  cur[l] = 1 - cur[l];
+  for (int k = 0; k < 5; k++) a.wsum[k] = (float)((double)(float)k + 0.0001);
+  return a;
 }
 
-void resid_restrict(MgHier &mg, std::vector<int> &cur, int l, double *norm2, cudaStream_t st) {
-  ProfScope ps_(l == 0 ? KC_RESTRICT_L0 : KC_RESTRICT_COARSE, st);
-  MgLevel &F = mg.lv[l];
-  MgLevel &C = mg.lv[l + 1];
-  RRArgs a{};
-  a.p = F.e[cur[l]];
-  a.rhs = F.rhs;
-  a.flag = F.flag;
-  a.w = F.w;
-  a.h = F.h;
-  a.pitch = F.pitch;
-  a.ihsq = 1.0f / F.hh / F.hh;
-  a.rc = C.rhs;
-  a.cw = C.w;
-  a.ch = C.h;
-  a.cpitch = C.pitch;
-  a.norm2 = norm2;
-  dim3 grid((C.w + CTX - 1) / CTX, (C.h + CTY - 1) / CTY);
-  k_resid_restrict<<<grid, 256, 0, st>>>(a);
+void run_tail(MgHier &mg, int lt, cudaStream_t st) {
+  ProfScope ps_(KC_TAIL, st);
+  TailArgs a{};
+  int nl = mg.levels - 1 - lt;
+  a.nlev = nl;
+  size_t fw = 0, bw = 0;
+  for (int t = 0; t < nl; t++) {
+    MgLevel &L = mg.lv[lt + t];
+    TailLevel &T = a.L[t];
+    int n = L.w * L.h;
+    T.w = L.w;
+    T.h = L.h;
+    T.hh = L.hh;
+    T.ihsq = 1.0f / L.hh / L.hh;
+    T.oe = (int)fw;
+    fw += (n + 3) / 4 * 4;
+    T.orr = (int)fw;
+    fw += (n + 3) / 4 * 4;
+    T.orhs = (int)fw;
+    fw += (n + 3) / 4 * 4;
+    T.oc = (int)bw;
+    bw += (n + 15) / 16 * 16;
+    a.code[t] = L.code;
+    a.code_pitch[t] = L.pitch;
+  }
+  a.float_words = (int)fw;
+  MgLevel &top = mg.lv[lt];
+  a.rhs_top = top.rhs;
+  a.rhs_pitch = top.pitch;
+  a.e_top = top.e[0];
+  a.e_pitch = top.pitch;
+  for (int k = 0; k < 5; k++) a.wsum[k] = (float)((double)(float)k + 0.0001);
+  size_t smem = fw * 4 + bw;
+  k_mg_tail<<<1, dim3(32, 32), smem, st>>>(a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -411,17 +743,63 @@ void resid_restrict(MgHier &mg, std::vector<int> &cur, int l, double *norm2, cud
 // MG::solveLevel, pressure_solver.cpp:201-248.
 void solve_level(MgHier &mg, std::vector<int> &cur, int l, bool zgbc, cudaStream_t st) {
   bool bc = zgbc && l == 0;
-  if (l == mg.levels - 2) {
-    smooth(mg, cur, l, 5, false, l > 0, nullptr, 0, 1.0f, st);
+  MgLevel &L = mg.lv[l];
+  if (l >= 1 && l == mg.tail_top) {
+    run_tail(mg, l, st);
+    cur[l] = 0;
     return;
   }
-  smooth(mg, cur, l, 3, bc, l > 0, nullptr, 0, 1.0f, st);
-  resid_restrict(mg, cur, l, nullptr, st);
+  if (l == mg.levels - 2) {
+    ProfScope ps_(l == 0 ? KC_SMOOTH_L0 : (l == 1 ? KC_SMOOTH_L1 : KC_SMOOTH_COARSE), st);
+    MgArgs a = level_args(L, L.e[cur[l]], L.e[1 - cur[l]], 5, 1.0f);
+    a.zero_init = l > 0;
+    launch_mg(a, st);
+    cur[l] ^= 1;
+    return;
+  }
+  MgLevel &C = mg.lv[l + 1];
+  {
+    ProfScope ps_(l == 0 ? KC_SMOOTH_L0 : (l == 1 ? KC_SMOOTH_L1 : KC_SMOOTH_COARSE), st);
+    MgArgs a = level_args(L, L.e[cur[l]], L.e[1 - cur[l]], 3, 1.0f);
+    a.zgbc = bc;
+    a.zero_init = l > 0;
+    a.rc = C.rhs;
+    a.cw = C.w;
+    a.ch = C.h;
+    a.cpitch = C.pitch;
+    launch_mg(a, st);
+    cur[l] ^= 1;
+  }
   solve_level(mg, cur, l + 1, false, st);
-  smooth(mg, cur, l, 3, bc, false, &mg.lv[l + 1], cur[l + 1], 1.0f, st);
+  {
+    ProfScope ps_(l == 0 ? KC_SMOOTH_L0 : (l == 1 ? KC_SMOOTH_L1 : KC_SMOOTH_COARSE), st);
+    MgArgs a = level_args(L, L.e[cur[l]], L.e[1 - cur[l]], 3, 1.0f);
+    a.zgbc = bc;
+    a.ec = C.e[cur[l + 1]];
+    a.codec = C.code;
+    a.cpitch = C.pitch;
+    a.cw = C.w;
+    a.ch = C.h;
+    if (l == 0) a.norm2 = mg.post_norm2;
+    launch_mg(a, st);
+    cur[l] ^= 1;
+  }
 }
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+int choose_tail(const std::vector<MgLevel> &lv) {
+  int L = (int)lv.size();
+  for (int lt = 1; lt <= L - 2; lt++) {
+    size_t bytes = 0;
+    for (int t = lt; t <= L - 2; t++) {
+      size_t n = (size_t)lv[t].w * lv[t].h;
+      bytes += 3 * ((n + 3) / 4 * 4) * 4 + (n + 15) / 16 * 16;
+    }
+    if (bytes <= TAIL_SMEM_MAX && (size_t)lv[lt].w * lv[lt].h <= 8192) return lt;
+  }
+  return -1;
+}
 
 }  // namespace
 
@@ -444,12 +822,13 @@ void mg_alloc(MgHier &mg, int W, int H, float h0) {
     ch = nh;
   }
   if (lv.size() < 2) throw ArgError("grid too small for the multigrid hierarchy (need W, H >= 8)");
+  init_kernel_attributes();
   size_t total = 0;
   for (auto &L : lv) {
     size_t n = (size_t)L.pitch * L.h;
-    total += 3 * align256(n * 4) + align256(n);
+    total += 3 * align256(n * 4) + 2 * align256(n);
   }
-  total += 256;  // norm scalar
+  total += 512;  // norm scalars
   void *arena = nullptr;
   if (cudaMalloc(&arena, total) != cudaSuccess) {
     cudaGetLastError();
@@ -467,8 +846,12 @@ void mg_alloc(MgHier &mg, int W, int H, float h0) {
     p += align256(n * 4);
     L.flag = (uint8_t *)p;
     p += align256(n);
+    L.code = (uint8_t *)p;
+    p += align256(n);
   }
   mg.norm = (double *)p;
+  mg.post_norm2 = nullptr;
+  mg.tail_top = choose_tail(lv);
   mg.lv = lv;
   mg.levels = (int)lv.size();
   mg.arena = arena;
@@ -483,15 +866,21 @@ void mg_free(MgHier &mg) {
   mg.levels = 0;
 }
 
+void level_make_code(MgLevel &L, cudaStream_t st) {
+  dim3 grid((L.w + 31) / 32, (L.h + 7) / 8);
+  k_make_code<<<grid, dim3(32, 8), 0, st>>>(L.flag, L.code, L.w, L.h, L.pitch);
+  UBG_LAUNCH_CHECK();
+}
+
 void mg_update_fields(MgHier &mg, cudaStream_t st) {
+  ProfScope ps_(KC_COARSEN, st);
   for (int l = 1; l < mg.levels; l++) {
     MgLevel &F = mg.lv[l - 1], &C = mg.lv[l];
-    ProfScope ps_(KC_COARSEN, st);
     dim3 grid((C.w + 31) / 32, (C.h + 7) / 8);
     k_coarsen<<<grid, dim3(32, 8), 0, st>>>(F.flag, F.pitch, C.flag, C.w, C.h, C.pitch);
     UBG_LAUNCH_CHECK();
-    g_stats.launches++;
   }
+  for (int l = 0; l < mg.levels; l++) level_make_code(mg.lv[l], st);
 }
 
 void mg_fill_coarse_flags_one(MgHier &mg, cudaStream_t st) {
@@ -501,6 +890,7 @@ void mg_fill_coarse_flags_one(MgHier &mg, cudaStream_t st) {
     k_fill_u8<<<grid, dim3(32, 8), 0, st>>>(C.flag, C.w, C.h, C.pitch, 1);
     UBG_LAUNCH_CHECK();
   }
+  for (int l = 0; l < mg.levels; l++) level_make_code(mg.lv[l], st);
 }
 
 void mg_solve(MgHier &mg, bool zgbc, cudaStream_t st) {
@@ -521,18 +911,9 @@ void mg_set_h(MgHier &mg, float h0) {
 
 void level_rbgs(MgLevel &L, int &cur, float alpha, cudaStream_t st) {
   ProfScope ps_(KC_SMOOTH_L0, st);
-  SmoothArgs a{};
-  a.in = L.e[cur];
-  a.out = L.e[1 - cur];
-  a.rhs = L.rhs;
-  a.flag = L.flag;
-  a.w = L.w;
-  a.h = L.h;
-  a.pitch = L.pitch;
-  a.hh = L.hh;
-  a.alpha = alpha;
-  a.nsweeps = 1;
-  launch_smooth(a, st);
+  init_kernel_attributes();
+  MgArgs a = level_args(L, L.e[cur], L.e[1 - cur], 1, alpha);
+  launch_mg_t<56, 24, 4, false>(a, st);
   cur = 1 - cur;
 }
 

@@ -15,7 +15,7 @@ const char *kernel_class_name(int kc) {
   static const char *n[KC_COUNT] = {"vbc", "accum", "diffuse", "advect", "divergence", "sinks",
                                     "pbc", "gradient", "cfl", "smooth_l0", "smooth_coarse",
                                     "resid_restrict_l0", "resid_restrict_coarse", "coarsen",
-                                    "residual", "tracers", "other"};
+                                    "residual", "tracers", "other", "smooth_l1", "tail"};
   return (kc >= 0 && kc < KC_COUNT) ? n[kc] : "?";
 }
 
@@ -81,7 +81,7 @@ __device__ __forceinline__ float single_pbc(int bc, float a) {
 // value reads the old row-0 value of its neighbour.
 template <bool XPAR>
 __device__ void vbc_component(const float *s, float *b0, float *b1, int pitch, int w, int h,
-                              Bcs bc, int t) {
+                              Bcs bc, int t, float &m) {
   // XPAR: x-edges use VBCPar and y-edges VBCPer (vx); otherwise swapped (vy).
   auto edge_x = [&](int side_bc, float a, float b) {
     return XPAR ? vbc_par(side_bc, a, b) : vbc_per(side_bc, a, b);
@@ -93,6 +93,7 @@ __device__ void vbc_component(const float *s, float *b0, float *b1, int pitch, i
   auto put = [&](int x, int y, float v) {
     b0[(size_t)y * pitch + x] = v;
     b1[(size_t)y * pitch + x] = v;
+    m = fmaxf(m, fabsf(v));
   };
   auto p1 = [&](int x, int y) {
     if (x == 0) return edge_x(bc.w, S(1, y), S(0, y));
@@ -130,17 +131,23 @@ __device__ void vbc_component(const float *s, float *b0, float *b1, int pitch, i
   }
 }
 
-__global__ void k_vbc(VelBufs v, int fx, int fy, Bcs bc, int do_vx, int do_vy) {
+__global__ void k_vbc(VelBufs v, int fx, int fy, Bcs bc, int do_vx, int do_vy,
+                      unsigned int *umax_bits) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int W = v.W, H = v.H;
   int nx = (H - 2) + (W - 1);
+  float m = 0.0f;
   if (t < nx) {
-    if (do_vx)
-      vbc_component<true>(v.vx[fx], v.vx[0], v.vx[1], v.pitch, W - 1, H, bc, t);
-    return;
+    if (do_vx) vbc_component<true>(v.vx[fx], v.vx[0], v.vx[1], v.pitch, W - 1, H, bc, t, m);
+  } else if (do_vy) {
+    vbc_component<false>(v.vy[fy], v.vy[0], v.vy[1], v.pitch, W, H - 1, bc, t - nx, m);
   }
-  t -= nx;
-  if (do_vy) vbc_component<false>(v.vy[fy], v.vy[0], v.vy[1], v.pitch, W, H - 1, bc, t);
+  // max |boundary value| for the next step's CFL dt (interior faces come
+  // from the gradient kernel)
+  if (umax_bits) {
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(umax_bits, __float_as_uint(m));
+  }
 }
 
 // ---------------------------------------------- applyAccumulatedVelocity
@@ -157,56 +164,186 @@ __global__ void k_accum(float *vx, float *vy, float *ax, float *ay, int pitch, i
   }
 }
 
-// ---------------------------------------------------------------- diffuse
-// One Jacobi sweep, simulation.cpp:114-128 (vx) and 140-154 (vy).
-__global__ void k_diffuse(VelBufs v, int srcx, int srcy, const uint8_t *__restrict__ flag,
-                          const StepScalars *__restrict__ sc, int comps) {
+// ------------------------------------------------------------- face codes
+// vx face (x, y) sits between cells x and x+1; vy face (x, y) between cells
+// y and y+1.  Diffusion terms (simulation.cpp:118-126 and 144-152):
+//   vx: T1 = vx(x+1,y)*f(x+1,y)*f(x+2,y), T2 = vx(x-1,y)*f(x,y)*f(x-1,y),
+//       T3 uses fvn = f(x,y+1)*f(x-1,y+1), T4 uses fvs = f(x,y-1)*f(x-1,y-1)
+//   vy: T1 = vy(x,y-1)*f(x,y)*f(x,y-1), T2 = vy(x,y+1)*f(x,y+1)*f(x,y+2),
+//       T3 uses fve = f(x+1,y)*f(x+1,y+1), T4 uses fvw = f(x-1,y)*f(x-1,y+1)
+// FC_A reproduces the chunked advection loop (simulation.cpp:248-256,
+// 300-304): faces from x = 1 in chunks of 8 while the chunk start is below
+// width-8, a chunk skipped when none of its lanes passes the fluid test.
+__global__ void k_face_codes(const uint8_t *__restrict__ flag, uint8_t *cx, uint8_t *cy, int P,
+                             int W, int H) {
   int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-  int W = v.W, H = v.H, P = v.pitch;
-  float a = sc->a, den = sc->den;
-  if (blockIdx.z == 0) {
-    if (!(comps & 1) || x < 1 || x >= W - 2 || y < 1 || y >= H - 1) return;
-    const float *s = v.vx[srcx];
-    float c = ld(s, P, x, y);
-    float val = 0.0f;
-    val = val + ld(s, P, x + 1, y) * fl(flag, P, x + 1, y) * fl(flag, P, x + 2, y);
-    val = val + ld(s, P, x - 1, y) * fl(flag, P, x, y) * fl(flag, P, x - 1, y);
-    float fvn = fl(flag, P, x, y + 1) * fl(flag, P, x - 1, y + 1);
-    val = val + (ld(s, P, x, y + 1) * fvn + (1.0f - fvn) * -c);
-    float fvs = fl(flag, P, x, y - 1) * fl(flag, P, x - 1, y - 1);
-    val = val + (ld(s, P, x, y - 1) * fvs + (1.0f - fvs) * -c);
-    v.vx[1 - srcx][(size_t)y * P + x] =
-        fl(flag, P, x, y) * fl(flag, P, x + 1, y) * (c + a * val) / den;
+  auto F = [&](int xx, int yy) -> unsigned { return flag[(size_t)yy * P + xx]; };
+  if (x < W - 1 && y < H) {
+    unsigned c = 0;
+    if (x >= 1 && x < W - 2 && y >= 1 && y < H - 1) {
+      if (F(x, y) & F(x + 1, y)) c |= FC_M;
+      if (F(x + 1, y) & F(x + 2, y)) c |= FC_T1;
+      if (F(x, y) & F(x - 1, y)) c |= FC_T2;
+      if (F(x, y + 1) & F(x - 1, y + 1)) c |= FC_T3;
+      if (F(x, y - 1) & F(x - 1, y - 1)) c |= FC_T4;
+      int xs = 1 + ((x - 1) >> 3) * 8;
+      if (xs < (W - 1) - 8)
+        for (int i = 0; i < 8; i++)
+          if (F(xs - 1 + i, y) & F(xs + i, y)) {
+            c |= FC_A;
+            break;
+          }
+    }
+    cx[(size_t)y * P + x] = (uint8_t)c;
+  }
+  if (x < W && y < H - 1) {
+    unsigned c = 0;
+    if (x >= 1 && x < W - 1 && y >= 1) {
+      // rows 1..H-2: the advection loop also covers vy's last row H-2
+      if (F(x, y) & F(x, y + 1)) c |= FC_M;
+      if (y < H - 2) {
+        if (F(x, y) & F(x, y - 1)) c |= FC_T1;
+        if (F(x, y + 1) & F(x, y + 2)) c |= FC_T2;
+        if (F(x + 1, y) & F(x + 1, y + 1)) c |= FC_T3;
+        if (F(x - 1, y) & F(x - 1, y + 1)) c |= FC_T4;
+      }
+      int xs = 1 + ((x - 1) >> 3) * 8;
+      if (xs < W - 8)
+        for (int i = 0; i < 8; i++)
+          if (F(xs + i, y) & F(xs + i, y - 1)) {
+            c |= FC_A;
+            break;
+          }
+    }
+    cy[(size_t)y * P + x] = (uint8_t)c;
+  }
+}
+
+// ---------------------------------------------------------------- diffuse
+// One Jacobi sweep, simulation.cpp:114-128 (vx) and 140-154 (vy).  With
+// flags in {0, 1}: v*f*f is f*f ? v : 0, v*fv + (1-fv)*(-c) is fv ? v : -c,
+// and the running sum starts at +0, so the face codes give the reference's
+// values (a zero's sign aside).
+// Row-vector access: a thread handles 4 consecutive faces of one row with
+// float4 loads (x is a multiple of 4 and rows are 128-byte aligned); a block
+// of 64 x 4 threads covers 256 x 4 faces.
+constexpr int VX = 64, VY = 4;
+__device__ __forceinline__ float4 ld4(const float *p, int P, int x, int y) {
+  return __ldg(reinterpret_cast<const float4 *>(p + (size_t)y * P + x));
+}
+__device__ __forceinline__ float comp(const float4 &v, int j) {
+  return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ unsigned compu(const uchar4 &v, int j) {
+  return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+// Stores the faces of [x, x+4) that lie in [lo, hi] (a whole float4 when all do).
+__device__ __forceinline__ void st4_masked(float *row, int x, int lo, int hi, const float o[4]) {
+  if (x >= lo && x + 3 <= hi) {
+    *reinterpret_cast<float4 *>(row + x) = make_float4(o[0], o[1], o[2], o[3]);
   } else {
-    if (!(comps & 2) || x < 1 || x >= W - 1 || y < 1 || y >= H - 2) return;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (x + j >= lo && x + j <= hi) row[x + j] = o[j];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
+                                                 const StepScalars *__restrict__ sc, int comps) {
+  const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
+  const int W = v.W, H = v.H, P = v.pitch;
+  const float a = sc->a, den = sc->den;
+  if (blockIdx.z == 0) {
+    // vx: interior faces x in [1, W-3], y in [1, H-2]
+    if (!(comps & 1) || y < 1 || y >= H - 1 || x > W - 3 || x + 3 < 1) return;
+    const float *s = v.vx[srcx];
+    float4 C = ld4(s, P, x, y), N = ld4(s, P, x, y + 1), S = ld4(s, P, x, y - 1);
+    uchar4 K = __ldg(reinterpret_cast<const uchar4 *>(v.cx + (size_t)y * P + x));
+    float L = x >= 1 ? ld(s, P, x - 1, y) : 0.0f;
+    float R = x + 4 < W - 1 ? ld(s, P, x + 4, y) : 0.0f;
+    float o[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      unsigned k = compu(K, j);
+      float c = comp(C, j);
+      float t1 = j < 3 ? comp(C, j + 1) : R, t2 = j > 0 ? comp(C, j - 1) : L;
+      float val = 0.0f;
+      val = val + ((k & FC_T1) ? t1 : 0.0f);
+      val = val + ((k & FC_T2) ? t2 : 0.0f);
+      val = val + ((k & FC_T3) ? comp(N, j) : -c);
+      val = val + ((k & FC_T4) ? comp(S, j) : -c);
+      o[j] = (k & FC_M) ? (c + a * val) / den : 0.0f;
+    }
+    st4_masked(v.vx[1 - srcx] + (size_t)y * P, x, 1, W - 3, o);
+  } else {
+    // vy: interior faces x in [1, W-2], y in [1, H-3]
+    if (!(comps & 2) || y < 1 || y >= H - 2 || x > W - 2 || x + 3 < 1) return;
     const float *s = v.vy[srcy];
-    float c = ld(s, P, x, y);
-    float val = 0.0f;
-    val = val + ld(s, P, x, y - 1) * fl(flag, P, x, y) * fl(flag, P, x, y - 1);
-    val = val + ld(s, P, x, y + 1) * fl(flag, P, x, y + 1) * fl(flag, P, x, y + 2);
-    float fve = fl(flag, P, x + 1, y) * fl(flag, P, x + 1, y + 1);
-    val = val + (ld(s, P, x + 1, y) * fve + (1.0f - fve) * -c);
-    float fvw = fl(flag, P, x - 1, y) * fl(flag, P, x - 1, y + 1);
-    val = val + (ld(s, P, x - 1, y) * fvw + (1.0f - fvw) * -c);
-    v.vy[1 - srcy][(size_t)y * P + x] =
-        fl(flag, P, x, y) * fl(flag, P, x, y + 1) * (c + a * val) / den;
+    float4 C = ld4(s, P, x, y), N = ld4(s, P, x, y + 1), S = ld4(s, P, x, y - 1);
+    uchar4 K = __ldg(reinterpret_cast<const uchar4 *>(v.cy + (size_t)y * P + x));
+    float L = x >= 1 ? ld(s, P, x - 1, y) : 0.0f;
+    float R = x + 4 < W ? ld(s, P, x + 4, y) : 0.0f;
+    float o[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      unsigned k = compu(K, j);
+      float c = comp(C, j);
+      float t3 = j < 3 ? comp(C, j + 1) : R, t4 = j > 0 ? comp(C, j - 1) : L;
+      float val = 0.0f;
+      val = val + ((k & FC_T1) ? comp(S, j) : 0.0f);
+      val = val + ((k & FC_T2) ? comp(N, j) : 0.0f);
+      val = val + ((k & FC_T3) ? t3 : -c);
+      val = val + ((k & FC_T4) ? t4 : -c);
+      o[j] = (k & FC_M) ? (c + a * val) / den : 0.0f;
+    }
+    st4_masked(v.vy[1 - srcy] + (size_t)y * P, x, 1, W - 2, o);
   }
 }
 
 // ----------------------------------------------------------------- advect
-// CubicHermite (interpolators.hpp:78-85): Catmull-Rom coefficients of the
-// reference, evaluated as a Horner polynomial with fused multiply-adds.
-__device__ __forceinline__ float cubic_hermite(float t, float A, float B, float C, float D) {
-  float a = ((-0.5f * A + 1.5f * B) - 1.5f * C) + 0.5f * D;
-  float b = ((A - 2.5f * B) + 2.0f * C) - 0.5f * D;
-  float c = 0.5f * (C - A);
-  return __fmaf_rn(__fmaf_rn(__fmaf_rn(a, t, b), t, c), t, B);
+// CubicHermite (interpolators.hpp:78-85) is the Catmull-Rom cubic; it is
+// evaluated through its four weights of t (the same polynomial, regrouped),
+// wA = t(-1/2 + t(1 - t/2)), wB = 1 + t^2(-5/2 + 3t/2),
+// wC = t(1/2 + t(2 - 3t/2)), wD = t^2(-1/2 + t/2), with explicit fused
+// multiply-adds, exactly as the CPU restatement does.
+struct CrW {
+  float a, b, c, d;
+};
+__device__ __forceinline__ CrW cr_weights(float t) {
+  float t2 = t * t;
+  CrW w;
+  w.a = t * __fmaf_rn(t, __fmaf_rn(-0.5f, t, 1.0f), -0.5f);
+  w.b = __fmaf_rn(t2, __fmaf_rn(1.5f, t, -2.5f), 1.0f);
+  w.c = t * __fmaf_rn(t, __fmaf_rn(-1.5f, t, 2.0f), 0.5f);
+  w.d = t2 * __fmaf_rn(0.5f, t, -0.5f);
+  return w;
+}
+__device__ __forceinline__ float cr_dot(const CrW &w, float A, float B, float C, float D) {
+  return __fmaf_rn(w.d, D, __fmaf_rn(w.c, C, __fmaf_rn(w.b, B, w.a * A)));
 }
 
-// bicubicSample (interpolators.hpp:92-206): clamp to [3, size-3], truncate,
-// vertical pass over 4 rows for 4 columns, then the horizontal pass.
-__device__ __forceinline__ float bicubic(const float *__restrict__ g, int pitch, int gw, int gh,
-                                         float cx, float cy) {
+// Catmull-Rom sample from 16 values (rows r0..r3 of a 4x4 stencil).
+__device__ __forceinline__ float bicubic16(const float *b, int stride, float sx, float sy) {
+  CrW wy = cr_weights(sy), wx = cr_weights(sx);
+  float col[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+    col[j] = cr_dot(wy, b[j], b[stride + j], b[2 * stride + j], b[3 * stride + j]);
+  return cr_dot(wx, col[0], col[1], col[2], col[3]);
+}
+
+// A staged window of one staggered component: region [sx0, sx0+SW) x
+// [sy0, sy0+SH) of the grid in shared memory.
+struct Win {
+  const float *s;
+  int sx0, sy0;
+};
+
+// bicubicSample (interpolators.hpp:92-206) reading the 4x4 stencil from the
+// shared-memory window when it lies inside, else from global memory.
+template <int SW, int SH>
+__device__ __forceinline__ float bicubic_win(const Win &wn, const float *__restrict__ g, int P,
+                                             int gw, int gh, float cx, float cy) {
   float hx = (float)gw - 3.0f, hy = (float)gh - 3.0f;
   cx = cx < hx ? cx : hx;
   cx = cx > 3.0f ? cx : 3.0f;
@@ -214,94 +351,121 @@ __device__ __forceinline__ float bicubic(const float *__restrict__ g, int pitch,
   cy = cy > 3.0f ? cy : 3.0f;
   int ix = (int)cx, iy = (int)cy;
   float sx = cx - (float)ix, sy = cy - (float)iy;
-  const float *r0 = g + (size_t)(iy - 1) * pitch + (ix - 1);
-  float col[4];
-#pragma unroll
-  for (int j = 0; j < 4; j++)
-    col[j] = cubic_hermite(sy, __ldg(r0 + j), __ldg(r0 + pitch + j), __ldg(r0 + 2 * pitch + j),
-                           __ldg(r0 + 3 * pitch + j));
-  return cubic_hermite(sx, col[0], col[1], col[2], col[3]);
+  int lx = ix - 1 - wn.sx0, ly = iy - 1 - wn.sy0;
+  if (lx >= 0 && lx + 3 < SW && ly >= 0 && ly + 3 < SH)
+    return bicubic16(wn.s + ly * SW + lx, SW, sx, sy);
+  return bicubic16(g + (size_t)(iy - 1) * P + (ix - 1), P, sx, sy);
 }
 
-// The reference advects in chunks of 8 faces from x = 1 while x < width-8
-// and skips a chunk when no lane passes the fluid test (simulation.cpp:248,
-// 254-256, 300, 302-304).  Returns whether face x of row y is advected.
-__device__ __forceinline__ bool advect_mask(const uint8_t *__restrict__ flag, int P, int W,
-                                            int x, int y, bool is_vx) {
-  int xs = 1 + ((x - 1) >> 3) * 8;
-  if (is_vx) {
-    if (!(xs < (W - 1) - 8)) return false;
-    const uint8_t *r = flag + (size_t)y * P;
-#pragma unroll
-    for (int i = 0; i < 8; i++)
-      if (__ldg(r + xs - 1 + i) && __ldg(r + xs + i)) return true;
-    return false;
-  } else {
-    if (!(xs < W - 8)) return false;
-    const uint8_t *r = flag + (size_t)y * P;
-    const uint8_t *rm = r - P;
-#pragma unroll
-    for (int i = 0; i < 8; i++)
-      if (__ldg(r + xs + i) && __ldg(rm + xs + i)) return true;
-    return false;
-  }
-}
+// advect, simulation.cpp:241-354.  A block handles the vx and vy faces of a
+// 64 x 16 tile of cells; both velocity components are staged in shared
+// memory with a 4-cell halo, which holds every stencil of a back-trace that
+// moves up to about one cell (the CFL-0.5 step moves at most half a cell);
+// longer traces read from global memory.
+constexpr int AD_TX = 64, AD_TY = 16, AD_H = 4;
+constexpr int AD_SW = AD_TX + 2 * AD_H, AD_SH = AD_TY + 2 * AD_H;
 
-__global__ void k_advect(VelBufs v, int srcx, int srcy, const uint8_t *__restrict__ flag,
-                         const StepScalars *__restrict__ sc) {
-  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-  int W = v.W, H = v.H, P = v.pitch;
+__global__ void __launch_bounds__(256) k_advect(VelBufs v, int srcx, int srcy,
+                                                const StepScalars *__restrict__ sc) {
+  __shared__ float sxv[AD_SH * AD_SW];
+  __shared__ float syv[AD_SH * AD_SW];
+  __shared__ uint8_t scx[AD_TY * AD_TX], scy[AD_TY * AD_TX];
+  const int W = v.W, H = v.H, P = v.pitch;
   const float *vx = v.vx[srcx];
   const float *vy = v.vy[srcy];
-  float chalf = sc->chalf, cfull = sc->cfull;
-  if (blockIdx.z == 0) {
-    // vx faces, simulation.cpp:247-298
-    if (x < 1 || x >= W - 2 || y < 1 || y >= H - 1) return;
-    if (!advect_mask(flag, P, W, x, y, true)) return;
-    float posx = (float)x + 0.5f, posy = (float)y;
-    float vx1 = ld(vx, P, x, y);
-    float vy1 = ((ld(vy, P, x, y) + ld(vy, P, x, y - 1)) + (ld(vy, P, x + 1, y) + ld(vy, P, x + 1, y - 1))) *
-                0.25f;
-    float midx = posx - vx1 * chalf;
-    float midy = posy - vy1 * chalf;
-    float vx2 = bicubic(vx, P, W - 1, H, midx - 0.5f, midy);
-    float vy2 = bicubic(vy, P, W, H - 1, midx, midy - 0.5f);
-    float endx = posx - vx2 * cfull;
-    float endy = posy - vy2 * cfull;
-    float r = bicubic(vx, P, W - 1, H, endx - 0.5f, endy);
-    v.vx[1 - srcx][(size_t)y * P + x] = r * fl(flag, P, x, y) * fl(flag, P, x + 1, y);
-  } else {
-    // vy faces, simulation.cpp:300-347 (rows 1..H-2 of the vx loop)
-    if (x < 1 || x >= W - 1 || y < 1 || y >= H - 1) return;
-    if (!advect_mask(flag, P, W, x, y, false)) return;
-    float posx = (float)x, posy = (float)y + 0.5f;
-    float vy1 = ld(vy, P, x, y);
-    // The reference reads vx at flat index x+1+y*(W-1): for x = W-2 that is
-    // element 0 of the next row.
-    float a0 = ld(vx, P, x, y), a1 = ld(vx, P, x, y - 1);
-    float a2 = (x + 1 < W - 1) ? ld(vx, P, x + 1, y) : ld(vx, P, 0, y + 1);
-    float a3 = (x + 1 < W - 1) ? ld(vx, P, x + 1, y - 1) : ld(vx, P, 0, y);
-    float vx1 = ((a0 + a1) + (a2 + a3)) * 0.25f;
-    float midx = posx - vx1 * chalf;
-    float midy = posy - vy1 * chalf;
-    float vx2 = bicubic(vx, P, W - 1, H, midx - 0.5f, midy);
-    float vy2 = bicubic(vy, P, W, H - 1, midx, midy - 0.5f);
-    float endx = posx - vx2 * cfull;
-    float endy = posy - vy2 * cfull;
-    float r = bicubic(vy, P, W, H - 1, endx, endy - 0.5f);
-    v.vy[1 - srcy][(size_t)y * P + x] = r * fl(flag, P, x, y) * fl(flag, P, x, y + 1);
+  const int X0 = blockIdx.x * AD_TX, Y0 = blockIdx.y * AD_TY;
+  const int sx0 = X0 - AD_H, sy0 = Y0 - AD_H;
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  for (int i = tid; i < AD_SH * AD_SW; i += 256) {
+    int ry = i / AD_SW, rx = i - ry * AD_SW;
+    int gx = sx0 + rx, gy = sy0 + ry;
+    float a = 0.0f, b = 0.0f;
+    if (gx >= 0 && gy >= 0) {
+      if (gx < W - 1 && gy < H) a = ld(vx, P, gx, gy);
+      if (gx < W && gy < H - 1) b = ld(vy, P, gx, gy);
+    }
+    sxv[i] = a;
+    syv[i] = b;
+  }
+  for (int i = tid; i < AD_TX * AD_TY; i += 256) {
+    int ty = i / AD_TX, tx = i - ty * AD_TX;
+    int x = X0 + tx, y = Y0 + ty;
+    uint8_t a = 0, b = 0;
+    if (x < W && y < H) {
+      a = __ldg(v.cx + (size_t)y * P + x);
+      b = __ldg(v.cy + (size_t)y * P + x);
+    }
+    scx[i] = a;
+    scy[i] = b;
+  }
+  __syncthreads();
+  const Win wx{sxv, sx0, sy0}, wy{syv, sx0, sy0};
+  const float chalf = sc->chalf, cfull = sc->cfull;
+  auto SX = [&](int x, int y) { return sxv[(y - sy0) * AD_SW + (x - sx0)]; };
+  auto SY = [&](int x, int y) { return syv[(y - sy0) * AD_SW + (x - sx0)]; };
+  float *outx = v.vx[1 - srcx], *outy = v.vy[1 - srcy];
+  for (int i = tid; i < AD_TX * AD_TY; i += 256) {
+    int ty = i / AD_TX, tx = i - ty * AD_TX;
+    int x = X0 + tx, y = Y0 + ty;
+    if (y < 1 || y >= H - 1 || x < 1) continue;
+    // vx face (x, y), simulation.cpp:247-298
+    if (x < W - 2) {
+      unsigned k = scx[i];
+      if (k & FC_A) {
+        float posx = (float)x + 0.5f, posy = (float)y;
+        float vx1 = SX(x, y);
+        float vy1 = ((SY(x, y) + SY(x, y - 1)) + (SY(x + 1, y) + SY(x + 1, y - 1))) * 0.25f;
+        float midx = posx - vx1 * chalf;
+        float midy = posy - vy1 * chalf;
+        float vx2 = bicubic_win<AD_SW, AD_SH>(wx, vx, P, W - 1, H, midx - 0.5f, midy);
+        float vy2 = bicubic_win<AD_SW, AD_SH>(wy, vy, P, W, H - 1, midx, midy - 0.5f);
+        float endx = posx - vx2 * cfull;
+        float endy = posy - vy2 * cfull;
+        float r = bicubic_win<AD_SW, AD_SH>(wx, vx, P, W - 1, H, endx - 0.5f, endy);
+        outx[(size_t)y * P + x] = (k & FC_M) ? r : 0.0f;
+      }
+    }
+    // vy face (x, y), simulation.cpp:300-347 (rows 1..H-2 of the vx loop)
+    if (x < W - 1) {
+      unsigned k = scy[i];
+      if (k & FC_A) {
+        float posx = (float)x, posy = (float)y + 0.5f;
+        float vy1 = SY(x, y);
+        // The reference reads vx at flat index x+1+y*(W-1): for x = W-2 that
+        // is element 0 of the next row.
+        float a2 = (x + 1 < W - 1) ? SX(x + 1, y) : ld(vx, P, 0, y + 1);
+        float a3 = (x + 1 < W - 1) ? SX(x + 1, y - 1) : ld(vx, P, 0, y);
+        float vx1 = ((SX(x, y) + SX(x, y - 1)) + (a2 + a3)) * 0.25f;
+        float midx = posx - vx1 * chalf;
+        float midy = posy - vy1 * chalf;
+        float vx2 = bicubic_win<AD_SW, AD_SH>(wx, vx, P, W - 1, H, midx - 0.5f, midy);
+        float vy2 = bicubic_win<AD_SW, AD_SH>(wy, vy, P, W, H - 1, midx, midy - 0.5f);
+        float endx = posx - vx2 * cfull;
+        float endy = posy - vy2 * cfull;
+        float r = bicubic_win<AD_SW, AD_SH>(wy, vy, P, W, H - 1, endx, endy - 0.5f);
+        outy[(size_t)y * P + x] = (k & FC_M) ? r : 0.0f;
+      }
+    }
   }
 }
 
 // ------------------------------------------------------------- divergence
-__global__ void k_divergence(const float *__restrict__ vx, const float *__restrict__ vy,
-                             float *__restrict__ f, int P, int W, int H,
-                             const StepScalars *__restrict__ sc) {
-  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-  if (x < 1 || x >= W - 1 || y < 1 || y >= H - 1) return;
-  float ih = sc->ih;
-  f[(size_t)y * P + x] =
-      -ih * (ld(vx, P, x, y) - ld(vx, P, x - 1, y) + ld(vy, P, x, y) - ld(vy, P, x, y - 1));
+__global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ vx,
+                                                    const float *__restrict__ vy,
+                                                    float *__restrict__ f, int P, int W, int H,
+                                                    const StepScalars *__restrict__ sc) {
+  const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
+  if (y < 1 || y >= H - 1 || x > W - 2 || x + 3 < 1) return;
+  const float ih = sc->ih;
+  float4 U = ld4(vx, P, x, y), V = ld4(vy, P, x, y), Vs = ld4(vy, P, x, y - 1);
+  float L = x >= 1 ? ld(vx, P, x - 1, y) : 0.0f;
+  float o[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    float um = j > 0 ? comp(U, j - 1) : L;
+    o[j] = -ih * (comp(U, j) - um + comp(V, j) - comp(Vs, j));
+  }
+  st4_masked(f + (size_t)y * P, x, 1, W - 2, o);
 }
 
 __global__ void k_sinks(float *f, int P, const SinkCell *cells, int n) {
@@ -340,27 +504,64 @@ __global__ void k_pbc(float *p, int P, int W, int H, Bcs bc) {
 }
 
 // ---------------------------------------------------------------- gradient
-__global__ void k_gradient(float *vx, float *vy, const float *__restrict__ p,
-                           const uint8_t *__restrict__ flag, int P, int W, int H,
-                           const StepScalars *__restrict__ sc) {
-  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
-  float ih = sc->ih;
-  size_t i = (size_t)y * P + x;
-  if (x >= 1 && x < W - 2 && y >= 1 && y < H - 1)
-    vx[i] = vx[i] - fl(flag, P, x, y) * fl(flag, P, x + 1, y) * ih * (ld(p, P, x + 1, y) - ld(p, P, x, y));
-  if (x >= 1 && x < W - 1 && y >= 1 && y < H - 2)
-    vy[i] = vy[i] - fl(flag, P, x, y) * fl(flag, P, x, y + 1) * ih * (ld(p, P, x, y + 1) - ld(p, P, x, y));
+// Pressure-gradient update; also folds max(|vx|, |vy|) of every interior
+// face (after the update) into *umax_bits for the next step's CFL dt.
+__global__ void __launch_bounds__(256) k_gradient(VelBufs v, int fx, int fy,
+                                                  const float *__restrict__ p,
+                                                  const StepScalars *__restrict__ sc,
+                                                  unsigned int *umax_bits) {
+  const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
+  const int W = v.W, H = v.H, P = v.pitch;
+  float m = 0.0f;
+  if (y >= 1 && y < H - 1 && x <= W - 2 && x + 3 >= 1) {
+    const float ih = sc->ih;
+    float *vx = v.vx[fx], *vy = v.vy[fy];
+    float4 P0 = ld4(p, P, x, y), PN = ld4(p, P, x, y + 1);
+    float PR = x + 4 < W ? ld(p, P, x + 4, y) : 0.0f;
+    float4 U = *reinterpret_cast<const float4 *>(vx + (size_t)y * P + x);
+    float4 V = *reinterpret_cast<const float4 *>(vy + (size_t)y * P + x);
+    uchar4 KX = __ldg(reinterpret_cast<const uchar4 *>(v.cx + (size_t)y * P + x));
+    uchar4 KY = __ldg(reinterpret_cast<const uchar4 *>(v.cy + (size_t)y * P + x));
+    float ox[4], oy[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      float p0 = comp(P0, j), pe = j < 3 ? comp(P0, j + 1) : PR;
+      float u = comp(U, j), w = comp(V, j);
+      bool inx = x + j >= 1 && x + j <= W - 3;
+      bool iny = x + j >= 1 && x + j <= W - 2 && y <= H - 3;
+      ox[j] = (inx && (compu(KX, j) & FC_M)) ? u - ih * (pe - p0) : u;
+      oy[j] = (iny && (compu(KY, j) & FC_M)) ? w - ih * (comp(PN, j) - p0) : w;
+      if (inx) m = fmaxf(m, fabsf(ox[j]));
+      if (iny) m = fmaxf(m, fabsf(oy[j]));
+    }
+    st4_masked(vx + (size_t)y * P, x, 1, W - 3, ox);
+    if (y <= H - 3) st4_masked(vy + (size_t)y * P, x, 1, W - 2, oy);
+  }
+  if (umax_bits) {
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(umax_bits, __float_as_uint(m));
+  }
 }
 
 // --------------------------------------------------------------------- CFL
-__global__ void k_umax(const float *__restrict__ vx, const float *__restrict__ vy, int P, int W,
-                       int H, unsigned int *umax_bits) {
-  int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+__global__ void __launch_bounds__(256) k_umax(const float *__restrict__ vx,
+                                              const float *__restrict__ vy, int P, int W, int H,
+                                              unsigned int *umax_bits) {
+  // grid-stride over rows; one atomic per block
   float m = 0.0f;
-  if (x < W - 1 && y < H) m = fabsf(ld(vx, P, x, y));
-  if (x < W && y < H - 1) m = fmaxf(m, fabsf(ld(vy, P, x, y)));
+  for (int y = blockIdx.y * 8 + threadIdx.y; y < H; y += gridDim.y * 8)
+    for (int x = blockIdx.x * 32 + threadIdx.x; x < W; x += gridDim.x * 32) {
+      if (x < W - 1) m = fmaxf(m, fabsf(ld(vx, P, x, y)));
+      if (y < H - 1) m = fmaxf(m, fabsf(ld(vy, P, x, y)));
+    }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(umax_bits, __float_as_uint(m));
+  __shared__ float red[8];
+  if (threadIdx.x == 0) red[threadIdx.y] = m;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    for (int i = 1; i < 8; i++) m = fmaxf(m, red[i]);
+    atomicMax(umax_bits, __float_as_uint(m));
+  }
 }
 
 __global__ void k_cfl_scalars(const unsigned int *umax_bits, float cfl, float h, float mu,
@@ -379,13 +580,23 @@ __global__ void k_cfl_scalars(const unsigned int *umax_bits, float cfl, float h,
 }
 
 inline dim3 grid2(int w, int h, int z = 1) { return dim3((w + BX - 1) / BX, (h + BY - 1) / BY, z); }
+inline dim3 grid_vec(int w, int h, int z = 1) {
+  return dim3((w + 4 * VX - 1) / (4 * VX), (h + VY - 1) / VY, z);
+}
 
 }  // namespace
 
-void launch_vbc(const VelBufs &v, int fx, int fy, Bcs bc, bool do_vx, bool do_vy, cudaStream_t st) {
+void launch_face_codes(const VelBufs &v, const uint8_t *flag, uint8_t *cx, uint8_t *cy,
+                       cudaStream_t st) {
+  k_face_codes<<<grid2(v.W, v.H), dim3(BX, BY), 0, st>>>(flag, cx, cy, v.pitch, v.W, v.H);
+  UBG_LAUNCH_CHECK();
+}
+
+void launch_vbc(const VelBufs &v, int fx, int fy, Bcs bc, bool do_vx, bool do_vy, cudaStream_t st,
+                unsigned int *umax_bits) {
   ProfScope ps_(KC_VBC, st);
   int n = (v.H - 2) + (v.W - 1) + (v.H - 3) + v.W;
-  k_vbc<<<(n + 255) / 256, 256, 0, st>>>(v, fx, fy, bc, do_vx, do_vy);
+  k_vbc<<<(n + 255) / 256, 256, 0, st>>>(v, fx, fy, bc, do_vx, do_vy, umax_bits);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -397,18 +608,18 @@ void launch_accum(const VelBufs &v, int fx, int fy, float *ax, float *ay, cudaSt
   g_stats.launches++;
 }
 
-void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const uint8_t *flag,
-                          const StepScalars *sc, int comps, cudaStream_t st) {
+void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, int comps,
+                          cudaStream_t st) {
   ProfScope ps_(KC_DIFFUSE, st);
-  k_diffuse<<<grid2(v.W, v.H, 2), dim3(BX, BY), 0, st>>>(v, srcx, srcy, flag, sc, comps);
+  k_diffuse<<<grid_vec(v.W, v.H, 2), dim3(VX, VY), 0, st>>>(v, srcx, srcy, sc, comps);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
 
-void launch_advect(const VelBufs &v, int srcx, int srcy, const uint8_t *flag,
-                   const StepScalars *sc, cudaStream_t st) {
+void launch_advect(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, cudaStream_t st) {
   ProfScope ps_(KC_ADVECT, st);
-  k_advect<<<grid2(v.W, v.H, 2), dim3(BX, BY), 0, st>>>(v, srcx, srcy, flag, sc);
+  dim3 grid((v.W + AD_TX - 1) / AD_TX, (v.H + AD_TY - 1) / AD_TY);
+  k_advect<<<grid, dim3(BX, BY), 0, st>>>(v, srcx, srcy, sc);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -416,7 +627,8 @@ void launch_advect(const VelBufs &v, int srcx, int srcy, const uint8_t *flag,
 void launch_divergence(const VelBufs &v, int fx, int fy, float *f, const StepScalars *sc,
                        cudaStream_t st) {
   ProfScope ps_(KC_DIVERGENCE, st);
-  k_divergence<<<grid2(v.W, v.H), dim3(BX, BY), 0, st>>>(v.vx[fx], v.vy[fy], f, v.pitch, v.W, v.H, sc);
+  k_divergence<<<grid_vec(v.W, v.H), dim3(VX, VY), 0, st>>>(v.vx[fx], v.vy[fy], f, v.pitch, v.W,
+                                                           v.H, sc);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -437,20 +649,27 @@ void launch_pbc(float *p, int pitch, int W, int H, Bcs bc, cudaStream_t st) {
   g_stats.launches++;
 }
 
-void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const uint8_t *flag,
-                     const StepScalars *sc, cudaStream_t st) {
+void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const StepScalars *sc,
+                     unsigned int *umax_bits, cudaStream_t st) {
   ProfScope ps_(KC_GRADIENT, st);
-  k_gradient<<<grid2(v.W, v.H), dim3(BX, BY), 0, st>>>(v.vx[fx], v.vy[fy], p, flag, v.pitch, v.W,
-                                                        v.H, sc);
+  k_gradient<<<grid_vec(v.W, v.H), dim3(VX, VY), 0, st>>>(v, fx, fy, p, sc, umax_bits);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
 
 void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, float pwidth,
-                unsigned int *umax_bits, StepScalars *sc, cudaStream_t st) {
+                unsigned int *umax_bits, StepScalars *sc, cudaStream_t st, bool umax_ready) {
   ProfScope ps_(KC_CFL, st);
+  if (umax_ready) {
+    k_cfl_scalars<<<1, 1, 0, st>>>(umax_bits, cfl, h, mu, pwidth, v.W, sc);
+    UBG_LAUNCH_CHECK();
+    g_stats.launches++;
+    return;
+  }
   UBG_CUDA(cudaMemsetAsync(umax_bits, 0, sizeof(unsigned int), st));
-  k_umax<<<grid2(v.W, v.H), dim3(BX, BY), 0, st>>>(v.vx[fx], v.vy[fy], v.pitch, v.W, v.H, umax_bits);
+  dim3 g((v.W + BX - 1) / BX, 64);
+  if (g.x > 16) g.x = 16;
+  k_umax<<<g, dim3(BX, BY), 0, st>>>(v.vx[fx], v.vy[fy], v.pitch, v.W, v.H, umax_bits);
   UBG_LAUNCH_CHECK();
   k_cfl_scalars<<<1, 1, 0, st>>>(umax_bits, cfl, h, mu, pwidth, v.W, sc);
   UBG_LAUNCH_CHECK();

@@ -73,23 +73,31 @@ struct VelBufs {
   float *vx[2];
   float *vy[2];
   int pitch, W, H;
+  // Per-face stencil codes (static per flag mask, pitched like the fields):
+  // FC_M = face mask flag*flag of the two cells, FC_T1..FC_T4 = weights of
+  // the four diffusion neighbour terms in the reference's order, FC_A = the
+  // reference's advection loop covers this face.
+  const uint8_t *cx, *cy;
 };
+constexpr unsigned FC_M = 1, FC_T1 = 2, FC_T2 = 4, FC_T3 = 8, FC_T4 = 16, FC_A = 32;
+// Builds the face codes from the cell flags.
+void launch_face_codes(const VelBufs &v, const uint8_t *flag, uint8_t *cx, uint8_t *cy,
+                       cudaStream_t st);
 
 // setVBCs (simulation.cpp:80-102): boundary values computed from the front
 // buffers (fx, fy), written to both buffers of each component.
 void launch_vbc(const VelBufs &v, int fx, int fy, Bcs bc, bool do_vx, bool do_vy,
-                cudaStream_t st);
+                cudaStream_t st, unsigned int *umax_bits = nullptr);
 // applyAccumulatedVelocity (simulation.cpp:376-396).
 void launch_accum(const VelBufs &v, int fx, int fy, float *ax, float *ay, cudaStream_t st);
 // One Jacobi diffusion sweep, buffer src -> buffer 1-src of each component
 // (simulation.cpp:112-129, 138-155); comps bit 0 = vx, bit 1 = vy.
-void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const uint8_t *flag,
-                          const StepScalars *sc, int comps, cudaStream_t st);
+void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, int comps,
+                          cudaStream_t st);
 // advect (simulation.cpp:241-354): reads buffer `src` of vx / vy, writes the
 // advected faces into buffer 1-src (faces the reference does not advect keep
 // their value).
-void launch_advect(const VelBufs &v, int srcx, int srcy, const uint8_t *flag,
-                   const StepScalars *sc, cudaStream_t st);
+void launch_advect(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, cudaStream_t st);
 // Divergence into f (simulation.cpp:166-171).
 void launch_divergence(const VelBufs &v, int fx, int fy, float *f, const StepScalars *sc,
                        cudaStream_t st);
@@ -97,19 +105,23 @@ void launch_divergence(const VelBufs &v, int fx, int fy, float *f, const StepSca
 void launch_sinks(float *f, int pitch, const SinkCell *cells, int n, cudaStream_t st);
 // setPBC (simulation.cpp:36-45).
 void launch_pbc(float *p, int pitch, int W, int H, Bcs bc, cudaStream_t st);
-// Pressure-gradient update (simulation.cpp:196-207).
-void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const uint8_t *flag,
-                     const StepScalars *sc, cudaStream_t st);
+// Pressure-gradient update (simulation.cpp:196-207); if umax_bits is set,
+// max(|u|) of the updated interior faces is folded into it (atomicMax on
+// the float bits).
+void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const StepScalars *sc,
+                     unsigned int *umax_bits, cudaStream_t st);
 // max(|vx|, |vy|) over the front buffers -> dt = cfl*h/max (extension) and
-// the derived scalars.
+// the derived scalars.  With umax_ready the maximum left in *umax_bits by
+// the previous step's gradient and boundary kernels is used as is.
 void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, float pwidth,
-                unsigned int *umax_bits, StepScalars *sc, cudaStream_t st);
+                unsigned int *umax_bits, StepScalars *sc, cudaStream_t st, bool umax_ready);
 
 // ------------------------------------------------------------ multigrid
 struct MgLevel {
   int w, h, pitch;
   float hh;            // grid spacing of this level
-  uint8_t *flag;       // w x h, pitched
+  uint8_t *flag;       // w x h, pitched, 0 / 1
+  uint8_t *code;       // per-cell stencil code (own flag + the 4 neighbours' flags)
   float *e[2];         // level 0: pressure ping-pong; coarse: error ping-pong
   float *rhs;          // level 0: f; coarse: restricted residual
 };
@@ -118,18 +130,21 @@ struct MgHier {
   int levels = 0;
   std::vector<MgLevel> lv;
   int cur0 = 0;                  // which e[] of level 0 holds p
+  int tail_top = -1;             // first level solved by the one-CTA tail kernel
   void *arena = nullptr;
   size_t arena_bytes = 0;
   double *norm = nullptr;        // device scalar for residual norms
-  // profiling hooks (optional)
-  cudaEvent_t ev_pair[2] = {nullptr, nullptr};
+  double *post_norm2 = nullptr;  // if set: ||r||^2 after each level-0 post-smoothing
 };
 
 // Allocates the hierarchy for a W x H level-0 grid with spacing h0.
 void mg_alloc(MgHier &mg, int W, int H, float h0);
 void mg_free(MgHier &mg);
-// MG::updateFields on the device: level 0 flag must already be set.
+// MG::updateFields on the device: level 0 flag must already be set; also
+// rebuilds the stencil codes of every level.
 void mg_update_fields(MgHier &mg, cudaStream_t st);
+// Stencil codes of one level from its flags.
+void level_make_code(MgLevel &L, cudaStream_t st);
 // Sets all coarse flags to 1.0 (MG(width, height) without a flag).
 void mg_fill_coarse_flags_one(MgHier &mg, cudaStream_t st);
 // One call of MG::solve(p, f, flag, h, zgbc) on level 0's e[cur0] / rhs.
@@ -155,7 +170,7 @@ extern thread_local LaunchStats g_stats;
 enum KernelClass {
   KC_VBC = 0, KC_ACCUM, KC_DIFFUSE, KC_ADVECT, KC_DIVERGENCE, KC_SINKS, KC_PBC, KC_GRADIENT,
   KC_CFL, KC_SMOOTH_L0, KC_SMOOTH_COARSE, KC_RESTRICT_L0, KC_RESTRICT_COARSE, KC_COARSEN,
-  KC_RESIDUAL, KC_TRACERS, KC_OTHER, KC_COUNT
+  KC_RESIDUAL, KC_TRACERS, KC_OTHER, KC_SMOOTH_L1, KC_TAIL, KC_COUNT
 };
 const char *kernel_class_name(int kc);
 
