@@ -20,6 +20,7 @@
 // so tiles never race on their halos.
 #include "ubg_internal.cuh"
 
+#include <cstdlib>
 #include <cstring>
 
 #define ALPHA_IS_ONE(a) ((a) == 1.0f)
@@ -167,7 +168,7 @@ struct Tile {
 // because x0 + y0 is even.  After half sweep i only cells within HALO - i of
 // the tile are still exact, so each half sweep updates just that cone.
 template <int TX, int TY, int HALO, bool ALPHA1, int NT>
-__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 6) k_mg(MgArgs a) {
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
   constexpr int NTY = NT / 32;
   using T = Tile<TX, TY, HALO>;
   constexpr int RX = T::RX, RY = T::RY, HX = T::HX;
@@ -181,49 +182,70 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 6) k_mg(MgArgs a) {
   const int x0 = blockIdx.x * TX - HALO, y0 = blockIdx.y * TY - HALO;
   const int w = a.w, h = a.h, P = a.pitch;
 
-  // ---- load p, f, code (float4 / uchar4 per thread; x0 is a multiple of 4);
-  // all of a thread's loads are issued before the first shared-memory store
+  // ---- load p, f, code (float4 / uchar4 per thread; x0 is a multiple of 4).
+  // One array at a time, all of a thread's loads of that array in flight
+  // together, into the red/black-split layout.
   constexpr int NQ = RY * (RX / 4), NIT = (NQ + NT - 1) / NT;
-  float4 pv[NIT], fv[NIT];
-  uchar4 cv[NIT];
+  auto load_split = [&](const float *src, float *dst, bool zero) {
+    float4 v[NIT];
 #pragma unroll
-  for (int it = 0; it < NIT; it++) {
-    int q = tid + it * NT;
-    int ry = q / (RX / 4), g = q - ry * (RX / 4);
-    int gx = x0 + 4 * g, gy = y0 + ry;
-    pv[it] = make_float4(0.f, 0.f, 0.f, 0.f);
-    fv[it] = pv[it];
-    cv[it] = make_uchar4(0, 0, 0, 0);
-    if (q < NQ && gy >= 0 && gy < h && gx >= 0 && gx < w) {
-      size_t gi = (size_t)gy * P + gx;
-      if (!a.zero_init) pv[it] = __ldg(reinterpret_cast<const float4 *>(a.in + gi));
-      fv[it] = __ldg(reinterpret_cast<const float4 *>(a.rhs + gi));
-      cv[it] = __ldg(reinterpret_cast<const uchar4 *>(a.code + gi));
+    for (int it = 0; it < NIT; it++) {
+      int q = tid + it * NT;
+      int ry = q / (RX / 4), g = q - ry * (RX / 4);
+      int gx = x0 + 4 * g, gy = y0 + ry;
+      v[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (!zero && q < NQ && gy >= 0 && gy < h && gx >= 0 && gx < w)
+        v[it] = __ldg(reinterpret_cast<const float4 *>(src + (size_t)gy * P + gx));
     }
-  }
 #pragma unroll
-  for (int it = 0; it < NIT; it++) {
-    int q = tid + it * NT;
-    if (q >= NQ) break;
-    int ry = q / (RX / 4), g = q - ry * (RX / 4);
-    int gx = x0 + 4 * g;
-    float4 p4 = pv[it], f4 = fv[it];
-    uchar4 c4 = cv[it];
-    if (gx + 3 >= w) {
-      if (gx + 1 >= w) { p4.y = 0.f; f4.y = 0.f; c4.y = 0; }
-      if (gx + 2 >= w) { p4.z = 0.f; f4.z = 0.f; c4.z = 0; }
-      p4.w = 0.f; f4.w = 0.f; c4.w = 0;
+    for (int it = 0; it < NIT; it++) {
+      int q = tid + it * NT;
+      if (q >= NQ) break;
+      int ry = q / (RX / 4), g = q - ry * (RX / 4);
+      int gx = x0 + 4 * g;
+      float4 p4 = v[it];
+      if (gx + 3 >= w) {
+        if (gx + 1 >= w) p4.y = 0.f;
+        if (gx + 2 >= w) p4.z = 0.f;
+        p4.w = 0.f;
+      }
+      int c0 = ry & 1;
+      *reinterpret_cast<float2 *>(dst + (c0 * RY + ry) * HX + 2 * g) = make_float2(p4.x, p4.z);
+      *reinterpret_cast<float2 *>(dst + ((c0 ^ 1) * RY + ry) * HX + 2 * g) = make_float2(p4.y, p4.w);
     }
-    int c0 = ry & 1;
-    int base0 = (c0 * RY + ry) * HX + 2 * g, base1 = ((c0 ^ 1) * RY + ry) * HX + 2 * g;
-    *reinterpret_cast<float2 *>(sp + base0) = make_float2(p4.x, p4.z);
-    *reinterpret_cast<float2 *>(sp + base1) = make_float2(p4.y, p4.w);
-    *reinterpret_cast<float2 *>(sf + base0) = make_float2(f4.x, f4.z);
-    *reinterpret_cast<float2 *>(sf + base1) = make_float2(f4.y, f4.w);
-    sc[base0] = c4.x;
-    sc[base0 + 1] = c4.z;
-    sc[base1] = c4.y;
-    sc[base1 + 1] = c4.w;
+  };
+  load_split(a.in, sp, a.zero_init != 0);
+  load_split(a.rhs, sf, false);
+  {
+    uchar4 cv[NIT];
+#pragma unroll
+    for (int it = 0; it < NIT; it++) {
+      int q = tid + it * NT;
+      int ry = q / (RX / 4), g = q - ry * (RX / 4);
+      int gx = x0 + 4 * g, gy = y0 + ry;
+      cv[it] = make_uchar4(0, 0, 0, 0);
+      if (q < NQ && gy >= 0 && gy < h && gx >= 0 && gx < w)
+        cv[it] = __ldg(reinterpret_cast<const uchar4 *>(a.code + (size_t)gy * P + gx));
+    }
+#pragma unroll
+    for (int it = 0; it < NIT; it++) {
+      int q = tid + it * NT;
+      if (q >= NQ) break;
+      int ry = q / (RX / 4), g = q - ry * (RX / 4);
+      int gx = x0 + 4 * g;
+      uchar4 c4 = cv[it];
+      if (gx + 3 >= w) {
+        if (gx + 1 >= w) c4.y = 0;
+        if (gx + 2 >= w) c4.z = 0;
+        c4.w = 0;
+      }
+      int c0 = ry & 1;
+      int base0 = (c0 * RY + ry) * HX + 2 * g, base1 = ((c0 ^ 1) * RY + ry) * HX + 2 * g;
+      sc[base0] = c4.x;
+      sc[base0 + 1] = c4.z;
+      sc[base1] = c4.y;
+      sc[base1 + 1] = c4.w;
+    }
   }
   __syncthreads();
 
@@ -307,9 +329,23 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 6) k_mg(MgArgs a) {
     __syncthreads();
   }
 
-  // ---- red-black sweeps
+  // ---- red-black sweeps: a thread updates 4 consecutive cells of one colour
+  // in one row (128-bit shared-memory accesses); G threads cover a row.
+  constexpr int G = HX / 4, RPP = NT / G;
+  static_assert(HX % 4 == 0 && NT % G == 0, "vector layout");
+  const int k0 = 4 * (tid % G), rsub = tid / G;
   const float hh = a.hh;
   const bool inner = x0 >= 1 && y0 >= 1 && x0 + RX <= w - 1 && y0 + RY <= h - 1;
+  // which of the thread's 4 cells may be smoothed (both parities):
+  // k >= 1 - par and k <= HX - 1 - par keep all neighbours in the region
+  auto cell_ok = [&](int k, int par, int gy) {
+    bool ok = k >= 1 - par && k <= HX - 1 - par;
+    if (!inner) {
+      int gx = x0 + 2 * k + par;
+      ok = ok && gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1;
+    }
+    return ok;
+  };
   int half = 0;
   for (int s = 0; s < a.nsweeps; s++) {
 #pragma unroll
@@ -319,36 +355,44 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 6) k_mg(MgArgs a) {
       const float *oth = sp + (color ^ 1) * RY * HX;
       const float *fs = sf + color * RY * HX;
       const uint8_t *cs = sc + color * RY * HX;
-      for (int ry = half + ty; ry <= RY - 1 - half; ry += NTY) {
+      for (int ry = half + rsub; ry <= RY - 1 - half; ry += RPP) {
         const int par = (ry + color) & 1;
         const int gy = y0 + ry;
+        const int row = ry * HX + k0;
+        const float4 o = *reinterpret_cast<const float4 *>(oth + row);
+        const float ex = par ? oth[row + 4] : oth[row - 1];
+        const float4 os = *reinterpret_cast<const float4 *>(oth + row - HX);
+        const float4 on = *reinterpret_cast<const float4 *>(oth + row + HX);
+        const float4 fv = *reinterpret_cast<const float4 *>(fs + row);
+        const float4 sv = *reinterpret_cast<const float4 *>(self + row);
+        const uchar4 cv = *reinterpret_cast<const uchar4 *>(cs + row);
+        const float W4[4] = {par ? o.x : ex, par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z};
+        const float E4[4] = {par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z, par ? ex : o.w};
+        const float S4[4] = {os.x, os.y, os.z, os.w}, N4[4] = {on.x, on.y, on.z, on.w};
+        const float F4[4] = {fv.x, fv.y, fv.z, fv.w}, P4[4] = {sv.x, sv.y, sv.z, sv.w};
+        const unsigned C4[4] = {cv.x, cv.y, cv.z, cv.w};
+        float out[4];
+        if (ALPHA1) {
+          const unsigned all = (unsigned)cv.x | ((unsigned)cv.y << 8) | ((unsigned)cv.z << 16) |
+                               ((unsigned)cv.w << 24);
+          // warp-uniform choice: all-fluid neighbourhoods take val / 4
+          if (__all_sync(__activemask(), all == 0x1f1f1f1fu)) {
 #pragma unroll
-        for (int kk = 0; kk < (HX + 31) / 32; kk++) {
-          const int k = kk * 32 + tx;
-          // all of a row is exact enough to compute (the cone is cut by rows
-          // only); the two end cells lack a neighbour in the region
-          bool ok = k >= 1 - par && k <= HX - 1 - par;
-          if (!inner) {
-            int gx = x0 + 2 * k + par;
-            ok = ok && gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1;
-          }
-          if (!ok) continue;
-          const int i = ry * HX + k;
-          const unsigned c = cs[i];
-          const float pw = oth[i - 1 + par], pe = oth[i + par];
-          const float ps = oth[i - HX], pn = oth[i + HX];
-          const float f = fs[i];
-          float v;
-          if (ALPHA1) {
-            if (c == (C_CENTER | C_W | C_E | C_S | C_N))
-              v = ((((pw + pe) + ps) + pn) + f * hh * hh) * 0.25f;
-            else
-              v = rb_update1(c, pw, pe, ps, pn, f, hh);
+            for (int j = 0; j < 4; j++)
+              out[j] = ((((W4[j] + E4[j]) + S4[j]) + N4[j]) + F4[j] * hh * hh) * 0.25f;
           } else {
-            v = rb_update_alpha(c, self[i], pw, pe, ps, pn, f, hh, a.alpha);
+#pragma unroll
+            for (int j = 0; j < 4; j++) out[j] = rb_update1(C4[j], W4[j], E4[j], S4[j], N4[j], F4[j], hh);
           }
-          self[i] = v;
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            out[j] = rb_update_alpha(C4[j], P4[j], W4[j], E4[j], S4[j], N4[j], F4[j], hh, a.alpha);
         }
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (!cell_ok(k0 + j, par, gy)) out[j] = P4[j];
+        *reinterpret_cast<float4 *>(self + row) = make_float4(out[0], out[1], out[2], out[3]);
       }
       __syncthreads();
     }
@@ -381,7 +425,10 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 6) k_mg(MgArgs a) {
 
   if (!a.rc && !a.norm2) return;
   // ---- residual on the tile grown by one cell (in place into f) ----------
-  double acc = 0.0;
+  // (per-thread partial sums of r^2 in FP32, a handful of terms each; the
+  // block and global sums are FP64.  No FP64 arithmetic in the cell loop:
+  // GB300's FP64 rate is a small fraction of FP32.)
+  float acc = 0.0f;
   const int rlo = a.rc ? HALO - 1 : HALO;
   const int rhix = a.rc ? HALO + TX : HALO + TX - 1, rhiy = a.rc ? HALO + TY : HALO + TY - 1;
 #pragma unroll
@@ -390,29 +437,43 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 6) k_mg(MgArgs a) {
     const float *oth = sp + (color ^ 1) * RY * HX;
     float *fs = sf + color * RY * HX;
     const uint8_t *cs = sc + color * RY * HX;
-    for (int ry = rlo + ty; ry <= rhiy; ry += NTY) {
+    for (int ry = rlo + rsub; ry <= rhiy; ry += RPP) {
       const int par = (ry + color) & 1;
       const int gy = y0 + ry;
-      for (int k = tx; k < HX; k += 32) {
-        const int rx = 2 * k + par, gx = x0 + rx;
-        if (rx < rlo || rx > rhix) continue;
-        const int i = ry * HX + k;
+      const int row = ry * HX + k0;
+      const float4 o = *reinterpret_cast<const float4 *>(oth + row);
+      const float ex = par ? oth[row + 4] : oth[row - 1];
+      const float4 os = *reinterpret_cast<const float4 *>(oth + row - HX);
+      const float4 on = *reinterpret_cast<const float4 *>(oth + row + HX);
+      const float4 fv = *reinterpret_cast<const float4 *>(fs + row);
+      const float4 sv = *reinterpret_cast<const float4 *>(self + row);
+      const uchar4 cv = *reinterpret_cast<const uchar4 *>(cs + row);
+      const float W4[4] = {par ? o.x : ex, par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z};
+      const float E4[4] = {par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z, par ? ex : o.w};
+      const float S4[4] = {os.x, os.y, os.z, os.w}, N4[4] = {on.x, on.y, on.z, on.w};
+      const float F4[4] = {fv.x, fv.y, fv.z, fv.w}, P4[4] = {sv.x, sv.y, sv.z, sv.w};
+      const unsigned C4[4] = {cv.x, cv.y, cv.z, cv.w};
+      float out[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int rx = 2 * (k0 + j) + par, gx = x0 + rx;
         float r = 0.0f;
-        if (gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1) {
-          r = resid1(cs[i], self[i], oth[i - 1 + par], oth[i + par], oth[i - HX], oth[i + HX], fs[i],
-                     a.ihsq);
+        if (rx >= rlo && rx <= rhix && gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1) {
+          r = resid1(C4[j], P4[j], W4[j], E4[j], S4[j], N4[j], F4[j], a.ihsq);
           if (a.norm2 && rx >= HALO && rx < HALO + TX && ry >= HALO && ry < HALO + TY)
-            acc += (double)r * (double)r;
+            acc = __fmaf_rn(r, r, acc);
         }
-        if (a.rc) fs[i] = r;
+        out[j] = r;
       }
+      if (a.rc) *reinterpret_cast<float4 *>(fs + row) = make_float4(out[0], out[1], out[2], out[3]);
     }
   }
   __syncthreads();
   if (a.norm2) {
     __shared__ double red[NTY];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (tx == 0) red[ty] = acc;
+    double dacc = (double)acc;
+    for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
+    if (tx == 0) red[ty] = dacc;
     __syncthreads();
     if (tid == 0) {
       double t = 0.0;
@@ -527,117 +588,151 @@ struct TailArgs {
   float wsum[5];
 };
 
-__global__ void __launch_bounds__(TAIL_THREADS) k_mg_tail(TailArgs a) {
+// A level may be worked by a team of threads (a prefix of the block, with
+// named barrier 1 or a warp barrier); measured on GB300, the whole block on
+// every level is fastest, so every level's team is the full block.
+__device__ __forceinline__ void team_sync(int team) {
+  if (team >= TAIL_THREADS)
+    __syncthreads();
+  else if (team > 32)
+    asm volatile("bar.sync 1, %0;" ::"r"(team) : "memory");
+  else
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *fm = reinterpret_cast<float *>(smem_raw);
   uint8_t *bm = smem_raw + (size_t)a.float_words * 4;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
   const int nl = a.nlev;
+  const float ws0 = a.wsum[0], ws1 = a.wsum[1], ws2 = a.wsum[2], ws3 = a.wsum[3], ws4 = a.wsum[4];
+  auto WS = [&](int k) {
+    return k == 0 ? ws0 : (k == 1 ? ws1 : (k == 2 ? ws2 : (k == 3 ? ws3 : ws4)));
+  };
+  auto team_of = [&](int t) {
+    (void)t;
+    return TAIL_THREADS;
+  };
 
   for (int t = 0; t < nl; t++) {
     const TailLevel &L = a.L[t];
-    for (int q = tid; q < L.w * L.h; q += TAIL_THREADS) {
-      int y = q / L.w, x = q - y * L.w;
-      bm[L.oc + q] = a.code[t][(size_t)y * a.code_pitch[t] + x];
-      fm[L.oe + q] = 0.0f;
-      if (t == 0) fm[L.orhs + q] = a.rhs_top[(size_t)y * a.rhs_pitch + x];
-    }
+    for (int y = ty; y < L.h; y += 32)
+      for (int x = tx; x < L.w; x += 32) {
+        int q = y * L.w + x;
+        bm[L.oc + q] = a.code[t][(size_t)y * a.code_pitch[t] + x];
+        fm[L.oe + q] = 0.0f;
+        if (t == 0) fm[L.orhs + q] = a.rhs_top[(size_t)y * a.rhs_pitch + x];
+      }
   }
   __syncthreads();
 
-  auto sweeps = [&](int t, int ns) {
+  auto sweeps = [&](int t, int ns, int team) {
     const TailLevel &L = a.L[t];
     float *e = fm + L.oe;
     const float *f = fm + L.orhs;
     const uint8_t *c = bm + L.oc;
-    const int w = L.w, hw2 = (w + 1) / 2;
+    const int w = L.w, hw2 = (w + 1) / 2, ystep = team / 32;
+    const float hh = L.hh;
     for (int s = 0; s < ns; s++) {
       for (int color = 1; color >= 0; color--) {
-        for (int y = 1 + ty; y < L.h - 1; y += 32) {
+        for (int y = 1 + ty; y < L.h - 1; y += ystep) {
           int par = (y + color) & 1;
           for (int j = tx; j < hw2; j += 32) {
             int x = 2 * j + par;
             if (x < 1 || x >= w - 1) continue;
             int i = y * w + x;
-            e[i] = rb_update1(c[i], e[i - 1], e[i + 1], e[i - w], e[i + w], f[i], L.hh);
+            unsigned ci = c[i];
+            float pw = e[i - 1], pe = e[i + 1], ps = e[i - w], pn = e[i + w], fi = f[i];
+            if (__all_sync(__activemask(), ci == (C_CENTER | C_W | C_E | C_S | C_N)))
+              e[i] = ((((pw + pe) + ps) + pn) + fi * hh * hh) * 0.25f;
+            else
+              e[i] = rb_update1(ci, pw, pe, ps, pn, fi, hh);
           }
         }
-        __syncthreads();
+        team_sync(team);
       }
     }
   };
 
   // down
   for (int t = 0; t < nl; t++) {
+    const int team = team_of(t);
+    if (tid >= team) continue;
+    const int ystep = team / 32;
     if (t == nl - 1) {
-      sweeps(t, 5);
+      sweeps(t, 5, team);
       break;
     }
-    sweeps(t, 3);
+    sweeps(t, 3, team);
     const TailLevel &L = a.L[t], &C = a.L[t + 1];
     float *e = fm + L.oe, *r = fm + L.orr;
     const float *f = fm + L.orhs;
     const uint8_t *c = bm + L.oc;
-    for (int q = tid; q < L.w * L.h; q += TAIL_THREADS) {
-      int y = q / L.w, x = q - y * L.w;
-      float rv = 0.0f;
-      if (x >= 1 && x < L.w - 1 && y >= 1 && y < L.h - 1)
-        rv = resid1(c[q], e[q], e[q - 1], e[q + 1], e[q - L.w], e[q + L.w], f[q], L.ihsq);
-      r[q] = rv;
-    }
-    __syncthreads();
-    float *rc = fm + C.orhs;
-    for (int q = tid; q < C.w * C.h; q += TAIL_THREADS) {
-      int Y = q / C.w, X = q - Y * C.w;
-      float v = 0.0f;
-      if (X >= 1 && X < C.w - 1 && Y >= 1 && Y < C.h - 1) {
-        const float *R0 = r + (2 * Y) * L.w + 2 * X;
-        v = (R0[-L.w - 1] * 1.0f + R0[-L.w] * 2.0f) + R0[-L.w + 1] * 1.0f;
-        v = v + ((R0[-1] * 2.0f + R0[0] * 4.0f) + R0[1] * 2.0f);
-        v = v + ((R0[L.w - 1] * 1.0f + R0[L.w] * 2.0f) + R0[L.w + 1] * 1.0f);
-        v = v * (1.0f / 16.0f);
+    for (int y = ty; y < L.h; y += ystep)
+      for (int x = tx; x < L.w; x += 32) {
+        int q = y * L.w + x;
+        float rv = 0.0f;
+        if (x >= 1 && x < L.w - 1 && y >= 1 && y < L.h - 1)
+          rv = resid1(c[q], e[q], e[q - 1], e[q + 1], e[q - L.w], e[q + L.w], f[q], L.ihsq);
+        r[q] = rv;
       }
-      rc[q] = v;
-    }
-    __syncthreads();
+    team_sync(team);
+    float *rc = fm + C.orhs;
+    for (int Y = ty; Y < C.h; Y += ystep)
+      for (int X = tx; X < C.w; X += 32) {
+        float v = 0.0f;
+        if (X >= 1 && X < C.w - 1 && Y >= 1 && Y < C.h - 1) {
+          const float *R0 = r + (2 * Y) * L.w + 2 * X;
+          v = (R0[-L.w - 1] * 1.0f + R0[-L.w] * 2.0f) + R0[-L.w + 1] * 1.0f;
+          v = v + ((R0[-1] * 2.0f + R0[0] * 4.0f) + R0[1] * 2.0f);
+          v = v + ((R0[L.w - 1] * 1.0f + R0[L.w] * 2.0f) + R0[L.w + 1] * 1.0f);
+          v = v * (1.0f / 16.0f);
+        }
+        rc[Y * C.w + X] = v;
+      }
+    team_sync(team);
   }
   // up
   for (int t = nl - 2; t >= 0; t--) {
+    const int team = team_of(t);
+    if (tid >= team) continue;
+    const int ystep = team / 32;
+    team_sync(team);  // the coarser level's team has finished
     const TailLevel &L = a.L[t], &C = a.L[t + 1];
     float *e = fm + L.oe;
     const float *ec = fm + C.oe;
     const uint8_t *c = bm + L.oc, *cc = bm + C.oc;
-    for (int q = tid; q < L.w * L.h; q += TAIL_THREADS) {
-      int y = q / L.w, x = q - y * L.w;
-      if (x < 1 || x >= L.w - 1 || y < 1 || y >= L.h - 1 || !(c[q] & C_CENTER)) continue;
-      int cx = x >> 1, cy = y >> 1;
-      auto E = [&](int xx, int yy) { return ec[yy * C.w + xx]; };
-      auto F = [&](int xx, int yy) { return (int)(cc[yy * C.w + xx] & 1u); };
-      bool xo = x & 1, yo = y & 1;
-      float ev;
-      if (!xo && !yo)
-        ev = E(cx, cy);
-      else if (xo && !yo)
-        ev = (x >= L.w - 2) ? 0.0f : (E(cx, cy) + E(cx + 1, cy)) / a.wsum[F(cx, cy) + F(cx + 1, cy)];
-      else if (!xo && yo)
-        ev = (y >= L.h - 2) ? 0.0f : (E(cx, cy) + E(cx, cy + 1)) / a.wsum[F(cx, cy) + F(cx, cy + 1)];
-      else
-        ev = (x >= L.w - 2 || y >= L.h - 2)
-                 ? 0.0f
-                 : (((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1)) /
-                       a.wsum[F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1)];
-      e[q] = e[q] + ev;
-    }
-    __syncthreads();
-    sweeps(t, 3);
+    for (int y = 1 + ty; y < L.h - 1; y += ystep)
+      for (int x = 1 + tx; x < L.w - 1; x += 32) {
+        int q = y * L.w + x;
+        if (!(c[q] & C_CENTER)) continue;
+        int cx = x >> 1, cy = y >> 1;
+        auto E = [&](int xx, int yy) { return ec[yy * C.w + xx]; };
+        auto F = [&](int xx, int yy) { return (int)(cc[yy * C.w + xx] & 1u); };
+        bool xo = x & 1, yo = y & 1;
+        float ev;
+        if (!xo && !yo)
+          ev = E(cx, cy);
+        else if (xo && !yo)
+          ev = (x >= L.w - 2) ? 0.0f : (E(cx, cy) + E(cx + 1, cy)) / WS(F(cx, cy) + F(cx + 1, cy));
+        else if (!xo && yo)
+          ev = (y >= L.h - 2) ? 0.0f : (E(cx, cy) + E(cx, cy + 1)) / WS(F(cx, cy) + F(cx, cy + 1));
+        else
+          ev = (x >= L.w - 2 || y >= L.h - 2)
+                   ? 0.0f
+                   : (((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1)) /
+                         WS(F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1));
+        e[q] = e[q] + ev;
+      }
+    team_sync(team);
+    sweeps(t, 3, team);
   }
+  __syncthreads();
   const TailLevel &L0 = a.L[0];
-  for (int q = tid; q < L0.w * L0.h; q += TAIL_THREADS) {
-    int y = q / L0.w, x = q - y * L0.w;
-    a.e_top[(size_t)y * a.e_pitch + x] = fm[L0.oe + q];
-  }
+  for (int y = ty; y < L0.h; y += 32)
+    for (int x = tx; x < L0.w; x += 32) a.e_top[(size_t)y * a.e_pitch + x] = fm[L0.oe + y * L0.w + x];
 }
-
 
 // ------------------------------------------------------------ launches
 template <int TX, int TY, int HALO, bool A1, int NT = 256>
@@ -653,17 +748,22 @@ template <int TX, int TY, int HALO, bool A1, int NT = 256>
 void set_smem_attr() {
   UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)Tile<TX, TY, HALO>::smem()));
+  // one carveout for every kernel of a V-cycle: no L1 / shared-memory
+  // reconfiguration between consecutive launches
+  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT>,
+                                cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 }
 
 void init_kernel_attributes() {
   static bool done = false;
   if (done) return;
-  set_smem_attr<112, 32, 8, true, 512>();
+  set_smem_attr<112, 50, 8, true, 512>();
   set_smem_attr<48, 16, 8, true>();
   set_smem_attr<40, 8, 12, true>();
   set_smem_attr<56, 24, 4, false>();
   UBG_CUDA(cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)TAIL_SMEM_MAX));
+  UBG_CUDA(cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   done = true;
 }
 
@@ -674,8 +774,8 @@ void launch_mg(const MgArgs &a, cudaStream_t st) {
     if (a.nsweeps != 1) throw ArgError("general alpha: one sweep per launch");
     launch_mg_t<56, 24, 4, false>(a, st);
   } else if (a.nsweeps <= 3) {
-    if (a.w >= 448)
-      launch_mg_t<112, 32, 8, true, 512>(a, st);
+    if (a.w >= 1200)
+      launch_mg_t<112, 50, 8, true, 512>(a, st);
     else
       launch_mg_t<48, 16, 8, true>(a, st);
   } else if (a.nsweeps <= 5) {
@@ -796,7 +896,7 @@ int choose_tail(const std::vector<MgLevel> &lv) {
       size_t n = (size_t)lv[t].w * lv[t].h;
       bytes += 3 * ((n + 3) / 4 * 4) * 4 + (n + 15) / 16 * 16;
     }
-    if (bytes <= TAIL_SMEM_MAX && (size_t)lv[lt].w * lv[lt].h <= 8192) return lt;
+    if (bytes <= TAIL_SMEM_MAX && (size_t)lv[lt].w * lv[lt].h <= 2048) return lt;
   }
   return -1;
 }
