@@ -73,6 +73,8 @@ _SIGS = {
     "ubg_mg_solve": (C.c_int, [_P, _FP, _FP, _FP, C.c_float, C.c_int]),
     "ubg_mg_solve_device": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, C.c_int, C.c_float,
                                       C.c_int, _P]),
+    "ubg_mg_solve_noalloc": (C.c_int, [_P, C.c_int, _P, C.c_int, _P, C.c_int, C.c_int, C.c_int,
+                                       C.c_float, C.c_int, _P]),
     "ubg_rbgs": (C.c_int, [_FP, _FP, _FP, C.c_int, C.c_int, C.c_float, C.c_float]),
     "ubg_residual": (C.c_int, [_FP, _FP, _FP, _FP, C.c_int, C.c_int, C.c_float,
                                C.POINTER(C.c_double)]),

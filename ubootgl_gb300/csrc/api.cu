@@ -16,8 +16,12 @@
 using namespace ubg;
 
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
+
+void ubg::set_last_error(const std::string &msg) { g_err = msg; }
+
+namespace {
 
 int fail(int code, const std::string &msg) {
   g_err = msg;

@@ -903,8 +903,8 @@ int choose_tail(const std::vector<MgLevel> &lv) {
 
 }  // namespace
 
-void mg_alloc(MgHier &mg, int W, int H, float h0) {
-  mg_free(mg);
+namespace {
+std::vector<MgLevel> level_shapes(int W, int H, float h0) {
   int cw = W, ch = H;
   float hh = h0;
   std::vector<MgLevel> lv;
@@ -922,19 +922,23 @@ void mg_alloc(MgHier &mg, int W, int H, float h0) {
     ch = nh;
   }
   if (lv.size() < 2) throw ArgError("grid too small for the multigrid hierarchy (need W, H >= 8)");
-  init_kernel_attributes();
+  return lv;
+}
+}  // namespace
+
+size_t mg_arena_bytes(int W, int H) {
   size_t total = 0;
-  for (auto &L : lv) {
+  for (auto &L : level_shapes(W, H, 1.0f)) {
     size_t n = (size_t)L.pitch * L.h;
     total += 3 * align256(n * 4) + 2 * align256(n);
   }
-  total += 512;  // norm scalars
-  void *arena = nullptr;
-  if (cudaMalloc(&arena, total) != cudaSuccess) {
-    cudaGetLastError();
-    throw std::bad_alloc();
-  }
-  UBG_CUDA(cudaMemset(arena, 0, total));
+  return total + 512;  // norm scalars
+}
+
+void mg_bind(MgHier &mg, int W, int H, float h0, void *arena, size_t bytes) {
+  std::vector<MgLevel> lv = level_shapes(W, H, h0);
+  if (bytes < mg_arena_bytes(W, H)) throw ArgError("multigrid arena too small");
+  init_kernel_attributes();
   char *p = (char *)arena;
   for (auto &L : lv) {
     size_t n = (size_t)L.pitch * L.h;
@@ -954,9 +958,22 @@ void mg_alloc(MgHier &mg, int W, int H, float h0) {
   mg.tail_top = choose_tail(lv);
   mg.lv = lv;
   mg.levels = (int)lv.size();
-  mg.arena = arena;
-  mg.arena_bytes = total;
+  mg.arena = nullptr;  // not owned
+  mg.arena_bytes = bytes;
   mg.cur0 = 0;
+}
+
+void mg_alloc(MgHier &mg, int W, int H, float h0) {
+  mg_free(mg);
+  size_t total = mg_arena_bytes(W, H);
+  void *arena = nullptr;
+  if (cudaMalloc(&arena, total) != cudaSuccess) {
+    cudaGetLastError();
+    throw std::bad_alloc();
+  }
+  UBG_CUDA(cudaMemset(arena, 0, total));
+  mg_bind(mg, W, H, h0, arena, total);
+  mg.arena = arena;
 }
 
 void mg_free(MgHier &mg) {

@@ -44,6 +44,9 @@ struct ArgError : std::runtime_error {
 
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
+// Sets the message returned by ubg_last_error() on the calling thread.
+void set_last_error(const std::string &msg);
+
 // ------------------------------------------------------------ step scalars
 // Quantities that depend on dt, formed exactly as the reference forms them
 // (simulation.cpp:105, 165, 242, 276, 286) in float.  They live in device
@@ -139,6 +142,10 @@ struct MgHier {
 
 // Allocates the hierarchy for a W x H level-0 grid with spacing h0.
 void mg_alloc(MgHier &mg, int W, int H, float h0);
+// Device bytes of the hierarchy of a W x H grid, and laying it out in a
+// caller-provided arena (not owned; nothing is allocated or cleared).
+size_t mg_arena_bytes(int W, int H);
+void mg_bind(MgHier &mg, int W, int H, float h0, void *arena, size_t bytes);
 void mg_free(MgHier &mg);
 // MG::updateFields on the device: level 0 flag must already be set; also
 // rebuilds the stencil codes of every level.
