@@ -181,6 +181,34 @@ int ubg_profile_read(ubg_sim *sim, double *smoother_ms, int *smoother_launches,
 int ubg_profile_class(ubg_sim *sim, int kc, const char **name, double *total_ms, int *count);
 int ubg_profile_reset(ubg_sim *sim);
 
+/* ------------------------------------------------------- display tracers */
+
+/* Display velocity texture of the simulation's current fields
+ * (VelocityTextures::updateFromStaggered + interp_shader.cs:14-34,
+ * velocity_textures.cpp:63-93), computed on the device into a headless
+ * buffer: vxy holds (2W-1) x (2H-1) pairs (vx, vy), mag (may be NULL) their
+ * lengths.  Host arrays; the call returns when they are filled. */
+int ubg_velocity_texture(ubg_sim *sim, float *vxy, float *mag);
+
+/* Fluid tracers (DrawTracersCS's GLTracers, draw_tracers_cs.cpp:131-169 and
+ * advect_tracer_points.cs:42-82) as device state bound to a simulation:
+ * ntracers rings of npoints positions, ring start / end pointers and ages.
+ * All start at zero; upload initial state with ubg_tracers_upload. */
+typedef struct ubg_tracers ubg_tracers;
+int ubg_tracers_create(ubg_sim *sim, int ntracers, int npoints, ubg_tracers **out);
+int ubg_tracers_destroy(ubg_tracers *tr);
+/* points: ntracers * npoints * 2 floats; start, end: ntracers each; ages:
+ * ntracers.  Any pointer may be NULL to skip that array. */
+int ubg_tracers_upload(ubg_tracers *tr, const float *points, const uint32_t *start,
+                       const uint32_t *end, const float *ages);
+int ubg_tracers_download(ubg_tracers *tr, float *points, uint32_t *start, uint32_t *end,
+                         float *ages);
+/* updateTracers (draw_tracers_cs.cpp:131-156): rebuilds the velocity texture
+ * from the simulation's current fields and advances every tracer by dt;
+ * rand_seed is the shader's rand_seed uniform.  Enqueued on the
+ * simulation's stream. */
+int ubg_tracers_step(ubg_tracers *tr, float dt, uint32_t rand_seed);
+
 /* --------------------------------------------------------------- class MG */
 
 /* MG(int width, int height) (pressure_solver.hpp:16-31), with every coarse

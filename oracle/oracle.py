@@ -73,9 +73,36 @@ def port_lib():
 def _bind_tracers(lib):
     P = C.POINTER(C.c_float)
     U = C.POINTER(C.c_uint32)
-    lib.ubo_tracers_f_step.argtypes = [P, P, C.c_int, C.c_int, P, C.c_int, P, C.c_int,
-                                       C.c_int, U, U, P, C.c_float, C.c_float, C.c_uint32]
+    lib.ubo_tracers_f_step.argtypes = [P, P, C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_int,
+                                       C.c_int, U, U, P, C.c_float, C.c_float, C.c_float,
+                                       C.c_uint32]
     lib.ubo_velocity_texture_f.argtypes = [P, P, C.c_int, C.c_int, P, P]
+
+
+def velocity_texture(vx, vy):
+    """interp_shader.cs restated: (vxy (2H-1, 2W-1, 2), mag (2H-1, 2W-1))."""
+    lib = port_lib()
+    H, W = vy.shape[0] + 1, vy.shape[1]
+    vx = np.ascontiguousarray(vx, np.float32)
+    vy = np.ascontiguousarray(vy, np.float32)
+    vxy = np.zeros((2 * H - 1, 2 * W - 1, 2), np.float32)
+    mag = np.zeros((2 * H - 1, 2 * W - 1), np.float32)
+    lib.ubo_velocity_texture_f(_fp(vx, C.c_float), _fp(vy, C.c_float), W, H,
+                               _fp(vxy, C.c_float), _fp(mag, C.c_float))
+    return vxy, mag
+
+
+def tracers_step(points, start, end, ages, vxy, flag, dt, pdim, rand_seed):
+    """advect_tracer_points.cs restated; arrays are updated in place."""
+    lib = port_lib()
+    ntr, npts = points.shape[0], points.shape[1]
+    th, tw = vxy.shape[0], vxy.shape[1]
+    nfy, nfx = flag.shape
+    lib.ubo_tracers_f_step(_fp(points, C.c_float), _fp(vxy, C.c_float), tw, th,
+                           _fp(np.ascontiguousarray(flag, np.float32), C.c_float), nfx, nfy, ntr,
+                           npts, start.ctypes.data_as(C.POINTER(C.c_uint32)),
+                           end.ctypes.data_as(C.POINTER(C.c_uint32)), _fp(ages, C.c_float),
+                           dt, pdim[0], pdim[1], rand_seed)
 
 
 def ref_available():

@@ -67,6 +67,13 @@ _SIGS = {
     "ubg_profile_class": (C.c_int, [_P, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
                                     C.POINTER(C.c_int)]),
     "ubg_profile_reset": (C.c_int, [_P]),
+    "ubg_velocity_texture": (C.c_int, [_P, _FP, _FP]),
+    "ubg_tracers_create": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(_P)]),
+    "ubg_tracers_destroy": (C.c_int, [_P]),
+    "ubg_tracers_upload": (C.c_int, [_P, _FP, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), _FP]),
+    "ubg_tracers_download": (C.c_int, [_P, _FP, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                       _FP]),
+    "ubg_tracers_step": (C.c_int, [_P, C.c_float, C.c_uint32]),
     "ubg_mg_create": (C.c_int, [C.c_int, C.c_int, _FP, C.POINTER(_P)]),
     "ubg_mg_destroy": (C.c_int, [_P]),
     "ubg_mg_update_fields": (C.c_int, [_P, _FP]),

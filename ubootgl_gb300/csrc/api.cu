@@ -792,6 +792,136 @@ int ubg_profile_reset(ubg_sim *s) {
   });
 }
 
+// ------------------------------------------------------- display tracers
+
+struct ubg_tracers {
+  ubg_sim *sim = nullptr;
+  int ntr = 0, npts = 0;
+  void *mem = nullptr;
+  float2 *points = nullptr;
+  uint32_t *start = nullptr, *end = nullptr;
+  float *ages = nullptr;
+  float2 *vxy = nullptr;
+  ~ubg_tracers() {
+    if (sim && sim->st) cudaStreamSynchronize(sim->st);
+    if (mem) cudaFree(mem);
+  }
+};
+
+int ubg_velocity_texture(ubg_sim *s, float *vxy, float *mag) {
+  return guarded([&] {
+    if (!s || !vxy) throw ArgError("null argument");
+    size_t n = (size_t)(2 * s->W - 1) * (2 * s->H - 1);
+    void *mem = nullptr;
+    UBG_CUDA(cudaMallocAsync(&mem, n * 12, s->st));
+    float2 *dv = (float2 *)mem;
+    float *dm = (float *)((char *)mem + n * 8);
+    launch_velocity_texture(s->v.vx[s->fx], s->v.vy[s->fy], s->P, s->W, s->H, dv, dm, s->st);
+    UBG_CUDA(cudaMemcpyAsync(vxy, dv, n * 8, cudaMemcpyDeviceToHost, s->st));
+    if (mag) UBG_CUDA(cudaMemcpyAsync(mag, dm, n * 4, cudaMemcpyDeviceToHost, s->st));
+    UBG_CUDA(cudaFreeAsync(mem, s->st));
+    s->sync();
+    return UBG_OK;
+  });
+}
+
+int ubg_tracers_create(ubg_sim *s, int ntracers, int npoints, ubg_tracers **out) {
+  return guarded([&] {
+    if (!s || !out) throw ArgError("null argument");
+    if (ntracers < 1 || npoints < 1 || (long long)ntracers * npoints > (1LL << 31))
+      throw ArgError("tracer counts out of range");
+    std::unique_ptr<ubg_tracers> t(new ubg_tracers());
+    t->sim = s;
+    t->ntr = ntracers;
+    t->npts = npoints;
+    size_t np = (size_t)ntracers * npoints * 8, nt = (size_t)ntracers * 4;
+    size_t ntex = (size_t)(2 * s->W - 1) * (2 * s->H - 1) * 8;
+    auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+    size_t total = al(np) + 3 * al(nt) + al(ntex);
+    if (cudaMalloc(&t->mem, total) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    UBG_CUDA(cudaMemsetAsync(t->mem, 0, total, s->st));
+    char *p = (char *)t->mem;
+    t->points = (float2 *)p; p += al(np);
+    t->start = (uint32_t *)p; p += al(nt);
+    t->end = (uint32_t *)p; p += al(nt);
+    t->ages = (float *)p; p += al(nt);
+    t->vxy = (float2 *)p;
+    s->sync();
+    *out = t.release();
+    return UBG_OK;
+  });
+}
+
+int ubg_tracers_destroy(ubg_tracers *t) {
+  return guarded([&] {
+    delete t;
+    return UBG_OK;
+  });
+}
+
+int ubg_tracers_upload(ubg_tracers *t, const float *points, const uint32_t *start,
+                       const uint32_t *end, const float *ages) {
+  return guarded([&] {
+    if (!t) throw ArgError("null handle");
+    cudaStream_t st = t->sim->st;
+    size_t np = (size_t)t->ntr * t->npts * 8, nt = (size_t)t->ntr * 4;
+    if (points) UBG_CUDA(cudaMemcpyAsync(t->points, points, np, cudaMemcpyHostToDevice, st));
+    if (start) UBG_CUDA(cudaMemcpyAsync(t->start, start, nt, cudaMemcpyHostToDevice, st));
+    if (end) UBG_CUDA(cudaMemcpyAsync(t->end, end, nt, cudaMemcpyHostToDevice, st));
+    if (ages) UBG_CUDA(cudaMemcpyAsync(t->ages, ages, nt, cudaMemcpyHostToDevice, st));
+    UBG_CUDA(cudaStreamSynchronize(st));
+    return UBG_OK;
+  });
+}
+
+int ubg_tracers_download(ubg_tracers *t, float *points, uint32_t *start, uint32_t *end,
+                         float *ages) {
+  return guarded([&] {
+    if (!t) throw ArgError("null handle");
+    cudaStream_t st = t->sim->st;
+    size_t np = (size_t)t->ntr * t->npts * 8, nt = (size_t)t->ntr * 4;
+    if (points) UBG_CUDA(cudaMemcpyAsync(points, t->points, np, cudaMemcpyDeviceToHost, st));
+    if (start) UBG_CUDA(cudaMemcpyAsync(start, t->start, nt, cudaMemcpyDeviceToHost, st));
+    if (end) UBG_CUDA(cudaMemcpyAsync(end, t->end, nt, cudaMemcpyDeviceToHost, st));
+    if (ages) UBG_CUDA(cudaMemcpyAsync(ages, t->ages, nt, cudaMemcpyDeviceToHost, st));
+    UBG_CUDA(cudaStreamSynchronize(st));
+    return UBG_OK;
+  });
+}
+
+int ubg_tracers_step(ubg_tracers *t, float dt, uint32_t rand_seed) {
+  return guarded([&] {
+    if (!t) throw ArgError("null handle");
+    ubg_sim *s = t->sim;
+    launch_velocity_texture(s->v.vx[s->fx], s->v.vy[s->fy], s->P, s->W, s->H, t->vxy, nullptr,
+                            s->st);
+    TracerArgs a{};
+    a.points = t->points;
+    a.start = t->start;
+    a.end = t->end;
+    a.ages = t->ages;
+    a.vxy = t->vxy;
+    a.tw = 2 * s->W - 1;
+    a.th = 2 * s->H - 1;
+    a.flag = s->flag();
+    a.nfx = s->W;
+    a.nfy = s->H;
+    a.fpitch = s->P;
+    a.ntracers = t->ntr;
+    a.npoints = t->npts;
+    a.dt = dt;
+    // pdim = (pwidth, pwidth * ny / nx), draw_tracers_cs.cpp:147
+    a.pdx = s->pwidth;
+    a.pdy = s->pwidth * (float)s->H / (float)s->W;
+    a.seed = rand_seed;
+    launch_tracers(a, s->st);
+    return UBG_OK;
+  });
+}
+
 // --------------------------------------------------------------- class MG
 
 int ubg_mg_create(int width, int height, const float *flag, ubg_mg **out) {

@@ -165,6 +165,26 @@ void level_rbgs(MgLevel &L, int &cur, float alpha, cudaStream_t st);
 // with its squared L2 norm accumulated into *norm2 (device double, may be null).
 void level_residual(const MgLevel &L, int cur, float *r, double *norm2, cudaStream_t st);
 
+// ------------------------------------------------------------- tracers
+struct TracerArgs {
+  float2 *points;       // ntracers x npoints ring of positions
+  uint32_t *start, *end;
+  float *ages;
+  const float2 *vxy;    // velocity texture, tw x th
+  int tw, th;
+  const uint8_t *flag;  // cell flags, nfx x nfy, row pitch fpitch
+  int nfx, nfy, fpitch;
+  int ntracers, npoints;
+  float dt, pdx, pdy;
+  uint32_t seed;
+};
+// interp_shader.cs: the (2W-1) x (2H-1) display texture (and magnitude if
+// mag is non-null) from the front velocity buffers.
+void launch_velocity_texture(const float *vx, const float *vy, int P, int W, int H, float2 *vxy,
+                             float *mag, cudaStream_t st);
+// advect_tracer_points.cs: one step of every tracer.
+void launch_tracers(const TracerArgs &a, cudaStream_t st);
+
 // Counters for the benchmark.
 struct LaunchStats {
   long launches = 0;

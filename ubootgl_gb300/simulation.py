@@ -202,6 +202,59 @@ class Simulation:
     vy_current = property(lambda s: s.get("vy_current"))
 
 
+class Tracers:
+    """Fluid tracers of a Simulation (draw_tracers_cs.cpp GLTracers +
+    advect_tracer_points.cs), device-resident."""
+
+    def __init__(self, sim, ntracers, npoints=30):
+        self._lib = L.load()
+        self.sim = sim
+        self.ntracers, self.npoints = int(ntracers), int(npoints)
+        h = C.c_void_p()
+        L.check(self._lib.ubg_tracers_create(sim._h, self.ntracers, self.npoints, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.ubg_tracers_destroy(self._h)
+            self._h = None
+
+    def upload(self, points=None, start=None, end=None, ages=None):
+        U = C.POINTER(C.c_uint32)
+        pts = None if points is None else _f32(points, (self.ntracers, self.npoints, 2))
+        st = None if start is None else np.ascontiguousarray(start, np.uint32)
+        en = None if end is None else np.ascontiguousarray(end, np.uint32)
+        ag = None if ages is None else _f32(ages, (self.ntracers,))
+        L.check(self._lib.ubg_tracers_upload(
+            self._h, None if pts is None else L.fptr(pts),
+            None if st is None else st.ctypes.data_as(U),
+            None if en is None else en.ctypes.data_as(U), None if ag is None else L.fptr(ag)))
+
+    def download(self):
+        U = C.POINTER(C.c_uint32)
+        pts = np.empty((self.ntracers, self.npoints, 2), np.float32)
+        st = np.empty(self.ntracers, np.uint32)
+        en = np.empty(self.ntracers, np.uint32)
+        ag = np.empty(self.ntracers, np.float32)
+        L.check(self._lib.ubg_tracers_download(self._h, L.fptr(pts), st.ctypes.data_as(U),
+                                               en.ctypes.data_as(U), L.fptr(ag)))
+        return pts, st, en, ag
+
+    def step(self, dt, rand_seed):
+        """updateTracers (draw_tracers_cs.cpp:131-156)."""
+        L.check(self._lib.ubg_tracers_step(self._h, dt, rand_seed))
+
+
+def velocity_texture(sim):
+    """interp_shader.cs on the simulation's current fields: (vxy, mag)."""
+    lib = L.load()
+    th, tw = 2 * sim.height - 1, 2 * sim.width - 1
+    vxy = np.empty((th, tw, 2), np.float32)
+    mag = np.empty((th, tw), np.float32)
+    L.check(lib.ubg_velocity_texture(sim._h, L.fptr(vxy), L.fptr(mag)))
+    return vxy, mag
+
+
 class MG:
     """class MG, pressure_solver.hpp:13-76.  MG(width, height) or MG(flag)."""
 
