@@ -245,6 +245,13 @@ def run_ours(args):
     e2e = end_to_end(sim, L, lib, W, H, max(3, min(args.steps, args.e2e_steps)), barrier, pg,
                      world, dev)
 
+    # ---- the mixed-precision solver on the same workload (extension)
+    modes = {}
+    if args.mode_steps > 0:
+        for prec in ("fp16", "bf16"):
+            modes["mixed_" + prec] = time_mode(L, lib, flag, vx, vy, prec, args.mode_steps,
+                                               args.warmup, dev)
+
     if rank != 0:
         return
     line = {
@@ -263,6 +270,7 @@ def run_ours(args):
         "roofline": kt["roofline"],
         "kernels": kt["detail"],
         "profiled_step_ms": kt["profiled_step_ms"],
+        "modes": modes,
     }
     if not args.no_cpu_baseline:
         val, info = time_cpu_step(W, H, budget_s=args.cpu_budget)
@@ -270,6 +278,40 @@ def run_ours(args):
                                 "cores": info["cores"], "kind": info["kind"],
                                 "sample": info["sample"]}
     print(json.dumps(line), flush=True)
+
+
+def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev):
+    """Whole steps with the mixed-precision pressure solver (2 defect
+    corrections, each one 16-bit V-cycle, in the captured step graph), timed
+    with CUDA events on the simulation's stream."""
+    import ctypes as C
+    import torch
+    from ubootgl_gb300.simulation import Simulation
+    H, W = flag.shape
+    sim = Simulation(flag, 1.0, 1e-4)
+    sim.set_options(solver_mode=L.SOLVE_FIXED, vcycles=2, precision=precision)
+    for n, a in (("vx", vx), ("vy", vy), ("vx_back", vx), ("vy_back", vy)):
+        sim.set(n, a)
+    stream = C.c_void_p()
+    L.check(lib.ubg_stream(sim._h, C.byref(stream)))
+    ext = torch.cuda.ExternalStream(stream.value, device=dev)
+    for _ in range(max(3, warmup)):
+        sim.step_cfl(0.5)
+    sim.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(steps):
+        sim.step_cfl(0.5)
+    e1.record(ext)
+    sim.sync()
+    ms = e0.elapsed_time(e1)
+    finite = bool(np.isfinite(sim.get("p")).all())
+    sim.close()
+    return {"value": round(W * H * steps / (ms / 1e3) / 1e6, 2), "unit": "Mcell-steps/s",
+            "ms_per_step": round(ms / steps, 5), "steps": steps,
+            "solver": "2 FP32 defect corrections, 16-bit (%s) V-cycle, FP64 norms and coarse "
+                      "solve" % precision, "fields_finite": finite}
 
 
 def working_set_bytes(W, H):
@@ -398,6 +440,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=30)
     ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--mode-steps", type=int, default=500,
+                    help="timed steps per mixed-precision mode (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -72,13 +72,22 @@ enum ubg_field {
  * V-cycles, simulation.cpp:189-190, and never looks at the residual). */
 enum ubg_solver_mode {
   UBG_SOLVE_FIXED = 0,     /* `vcycles` V-cycles (2 = the reference) */
-  UBG_SOLVE_TOLERANCE = 1  /* V-cycles until ||r||/||r0|| <= tol or max_vcycles */
+  UBG_SOLVE_TOLERANCE = 1  /* V-cycles until ||r|| <= tol * ||f|| (FP64 norms over the
+                              interior fluid cells) or max_vcycles.  The solver's
+                              system has zero-gradient edges everywhere and is
+                              singular, so this mode first subtracts the mean
+                              of f over the interior fluid cells: it solves the
+                              compatible part. */
 };
 
 /* Precision of the multigrid corrections (extension).  FP32 is the
- * reference's arithmetic.  MIXED_* run an FP32 defect-correction loop whose
- * inner V-cycle stores and smooths the error equation in FP16 / BF16, with
- * FP64 global norms and an FP64 coarsest-level solve. */
+ * reference's arithmetic.  MIXED_* run an FP32 defect-correction loop
+ * (residual, convergence test and p += e in FP32, norms in FP64) whose inner
+ * V-cycle stores the error equation in FP16 / BF16 on every level, computes
+ * in FP32 registers, and solves the coarse levels (<= 2048 cells) in FP64.
+ * In FIXED mode each V-cycle is one correction, and k corrections equal (in
+ * exact arithmetic) k V-cycles of the reference started from p with
+ * zero-gradient edges. */
 enum ubg_precision { UBG_FP32 = 0, UBG_MIXED_FP16 = 1, UBG_MIXED_BF16 = 2 };
 
 typedef struct ubg_options {
@@ -133,6 +142,11 @@ int ubg_step(ubg_sim *sim, float dt);
 int ubg_step_cfl(ubg_sim *sim, float cfl);
 int ubg_last_dt(ubg_sim *sim, float *dt);
 
+/* Pressure-solve statistics of the last step or projection (extension):
+ * V-cycles (mixed modes: corrections) run, and in TOLERANCE mode the final
+ * ||r|| / ||f * flag|| (else -1).  Host values; no synchronisation. */
+int ubg_solver_stats(ubg_sim *sim, int *vcycles, double *rel_residual);
+
 /* Individual stages of the step, for callers that drive them one by one and
  * for stage-wise parity tests.  `dt` sets the member Simulation::dt first. */
 int ubg_apply_accumulated_velocity(ubg_sim *sim); /* simulation.cpp:376-396 */
@@ -151,6 +165,47 @@ int ubg_add_sink(ubg_sim *sim, float x, float y, float strength);
  * (ubootgl_app.cpp:111-112): the coarse flags are rebuilt on the device. */
 int ubg_upload(ubg_sim *sim, int field, const float *src);
 int ubg_download(ubg_sim *sim, int field, float *dst);
+
+/* ------------------------------------------------ game-side field access */
+
+/* bilinearScatter into the accumulation fields (interpolators.hpp:29-40) as
+ * the floating items apply their force to the fluid
+ * (advect_floating_items.cpp:116-120, 239-244): for each of n items,
+ * xy[2i..2i+1] = pos / h (grid units) and v[2i..2i+1] the values to add;
+ * v.x is scattered into vx_accum at xy - (0.5, 0) and v.y into vy_accum at
+ * xy - (0, 0.5) (callers pass -deltaVec).  Coordinates are clamped as in the
+ * reference.  On the device with atomic adds: items whose stencils overlap
+ * sum in an unspecified order.  The next step applies the accumulation. */
+int ubg_scatter_accum(ubg_sim *sim, int n, const float *xy, const float *v);
+
+/* Simulation::bilinearVel (advect_floating_items.cpp:11-14) for n points
+ * xy (grid units, pos / h) on the device's current vx / vy: out[2i..2i+1]. */
+int ubg_sample_velocity(ubg_sim *sim, int n, const float *xy, float *out);
+
+/* Simulation::setGrids(c, val) (simulation.hpp:82-98) for n cells
+ * xy[2i..2i+1] with values vals[i] (0.0 or 1.0), in call order: the flag
+ * takes the last value, a cell set to 0.0 has its four faces (front
+ * buffers) and p zeroed; cells outside the grid are ignored.  The coarse
+ * flags and stencil codes are rebuilt (mg.updateFields), as the reference's
+ * callers do after editing the flag. */
+int ubg_set_grids(ubg_sim *sim, int n, const int *xy, const float *vals);
+
+/* UbootGlApp::shiftMap (ubootgl_app.cpp:245-298) on the device: vx, vy
+ * (both buffers from the front) and p move one column west, new_flag (the
+ * shifted terrain, width x height, 0.0 / 1.0) is applied cell by cell with
+ * setGrids, the inflow column is reset to 0.07 * height / inletArea *
+ * flag(0, y), and mg.updateFields runs. */
+int ubg_shift_map(ubg_sim *sim, const float *new_flag);
+
+/* Session snapshot / restore (extension, for eviction and checkpoints): a
+ * header (magic "UBGSNAP1", version 1, width, height, pwidth, mu, h, last dt,
+ * boundary types, sinks), then vx, vx back, vy, vy back, p, f, vx_accum,
+ * vy_accum as unpitched float arrays and the flag as bytes.  Restore needs a
+ * simulation of the same width and height; solver options are not part of
+ * a snapshot. */
+int ubg_snapshot_bytes(ubg_sim *sim, size_t *bytes);
+int ubg_snapshot(ubg_sim *sim, void *dst);
+int ubg_restore(ubg_sim *sim, const void *src);
 
 /* Multigrid of the simulation: number of levels, size and (float) flag of
  * one level (MG::flagcs, pressure_solver.hpp:72). */

@@ -42,6 +42,7 @@ def port_lib():
             for n in ("apply_accum", "diffuse", "advect", "set_vbcs", "set_pbc", "project"):
                 g(n).argtypes = [C.c_void_p]
             g("project_ncycles").argtypes = [C.c_void_p, C.c_int]
+            g("project_opts").argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
             g("sim_mg_solve").argtypes = [C.c_void_p, C.c_int]
             g("get_field").argtypes = [C.c_void_p, C.c_int, P]
             g("set_field").argtypes = [C.c_void_p, C.c_int, P]
@@ -138,6 +139,9 @@ def ref_lib():
         lib.ref_residual.restype = C.c_float
         lib.ref_residual.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_float]
         lib.ref_set_threads.argtypes = [C.c_int]
+        lib.ref_bilinear_sample_n.argtypes = [P, C.c_int, C.c_int, C.c_int, P, P]
+        lib.ref_bilinear_scatter_n.argtypes = [P, C.c_int, C.c_int, C.c_int, P, P]
+        lib.ref_set_grids.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float]
         _ref = lib
     return _ref
 
@@ -201,6 +205,13 @@ class PortSim:
 
     def mg_solve(self, zgbc=True):
         self._fn("sim_mg_solve")(self.h_, 1 if zgbc else 0)
+
+    def project(self, ncycles=2, meanfree=False, zgbc_first=False):
+        """project() with `ncycles` V-cycles (simulation.cpp:164-208).
+        meanfree: subtract the mean of f over the interior fluid cells first
+        (the tolerance modes' compatible system); zgbc_first: zero-gradient
+        edges on p before the first V-cycle (the mixed solver's start)."""
+        self._fn("project_opts")(self.h_, ncycles, 1 if meanfree else 0, 1 if zgbc_first else 0)
 
     def add_sink(self, x, y, z):
         self._fn("add_sink")(self.h_, x, y, z)
@@ -273,6 +284,9 @@ class RefSim:
     def add_sink(self, x, y, z):
         self.lib.ref_add_sink(self.h_, x, y, z)
 
+    def set_grids(self, x, y, val):
+        self.lib.ref_set_grids(self.h_, x, y, val)
+
 
 def port_mg_solve(p, f, flag, h, zgbc=False, coarse_flag=None, dtype=np.float32):
     """Standalone MG::solve on copies (class MG, pressure_solver.hpp:13-76).
@@ -325,3 +339,97 @@ def port_residual(p, f, flag, h, dtype=np.float32):
 
 def set_threads(n):
     port_lib().ubo_omp_set_threads(n)
+
+
+# ---------------------------------------------------------------------------
+# Game-side field access, restated in numpy float32 scalar arithmetic in the
+# reference's evaluation order (test infrastructure only).
+
+def _f32(v):
+    return np.float32(v)
+
+
+def bilinear_sample(grid, cx, cy):
+    """bilinearSample, interpolators.hpp:11-27 (grid indexed [y, x])."""
+    gh, gw = grid.shape
+    cx = min(max(_f32(cx), _f32(0.0)), _f32(gw) - _f32(1.1))
+    cy = min(max(_f32(cy), _f32(0.0)), _f32(gh) - _f32(1.1))
+    ix, iy = int(cx), int(cy)
+    sx, sy = cx - np.floor(cx), cy - np.floor(cy)
+    v1, v2 = grid[iy, ix], grid[iy, ix + 1]
+    v3, v4 = grid[iy + 1, ix], grid[iy + 1, ix + 1]
+    vm1 = v1 + (v2 - v1) * sx
+    vm2 = v3 + (v4 - v3) * sx
+    return vm1 + (vm2 - vm1) * sy
+
+
+def bilinear_scatter(grid, cx, cy, v):
+    """bilinearScatter, interpolators.hpp:29-40 (in place)."""
+    gh, gw = grid.shape
+    cx = min(max(_f32(cx), _f32(0.0)), _f32(gw) - _f32(1.1))
+    cy = min(max(_f32(cy), _f32(0.0)), _f32(gh) - _f32(1.1))
+    ix, iy = int(cx), int(cy)
+    sx, sy = cx - np.floor(cx), cy - np.floor(cy)
+    ax, ay = _f32(1.0) - sx, _f32(1.0) - sy
+    v = _f32(v)
+    grid[iy + 1, ix + 1] += sx * sy * v
+    grid[iy + 1, ix] += ax * sy * v
+    grid[iy, ix + 1] += sx * ay * v
+    grid[iy, ix] += ax * ay * v
+
+
+def bilinear_vel(vx, vy, cx, cy):
+    """Simulation::bilinearVel, advect_floating_items.cpp:11-14."""
+    return (bilinear_sample(vx, _f32(cx) - _f32(0.5), _f32(cy) - _f32(0.0)),
+            bilinear_sample(vy, _f32(cx) - _f32(0.0), _f32(cy) - _f32(0.5)))
+
+
+def scatter_items(vx_accum, vy_accum, xy, v):
+    """The floating items' force transfer, advect_floating_items.cpp:116-120."""
+    for (cx, cy), (a, b) in zip(xy, v):
+        bilinear_scatter(vx_accum, _f32(cx) - _f32(0.5), _f32(cy) - _f32(0.0), a)
+        bilinear_scatter(vy_accum, _f32(cx) - _f32(0.0), _f32(cy) - _f32(0.5), b)
+
+
+def set_grids(fields, x, y, val):
+    """Simulation::setGrids, simulation.hpp:82-98; fields: dict of flag, vx,
+    vy, p (front buffers), modified in place."""
+    flag = fields["flag"]
+    H, W = flag.shape
+    if not (x >= 0 and y >= 0 and x < W and y < H):
+        return
+    flag[y, x] = val
+    if val == 0:
+        if x < W - 1:
+            fields["vx"][y, x] = 0.0
+        if x > 0:
+            fields["vx"][y, x - 1] = 0.0
+        if y < H - 1:
+            fields["vy"][y, x] = 0.0
+        if y > 0:
+            fields["vy"][y - 1, x] = 0.0
+        fields["p"][y, x] = 0.0
+
+
+def shift_map(fields, new_flag):
+    """UbootGlApp::shiftMap, ubootgl_app.cpp:245-298; fields: dict of vx,
+    vx_back, vy, vy_back, p, flag (float32), modified in place."""
+    for c in ("vx", "vy"):
+        f, b = fields[c], fields[c + "_back"]
+        w = f.shape[1]
+        for x in range(2, w):
+            f[:, x - 1] = f[:, x]
+            b[:, x - 1] = f[:, x]
+    p = fields["p"]
+    for x in range(1, p.shape[1]):
+        p[:, x - 1] = p[:, x]
+    H, W = new_flag.shape
+    for y in range(H):
+        for x in range(W):
+            set_grids(fields, x, y, new_flag[y, x])
+    area = np.float32(1.0)
+    for y in range(fields["vy"].shape[0]):
+        area = np.float32(area + fields["flag"][y, 0])
+    for y in range(fields["vx"].shape[0]):
+        u = np.float32(np.float32(0.07) * np.float32(H)) / area
+        fields["vx"][y, 0] = fields["vx_back"][y, 0] = np.float32(u * fields["flag"][y, 0])

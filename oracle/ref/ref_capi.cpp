@@ -5,6 +5,7 @@
 #include <omp.h>
 #include <cstring>
 #include "simulation.hpp"
+#include "interpolators.hpp"
 
 namespace {
 enum { F_VX = 0, F_VY = 1, F_VX_BACK = 2, F_VY_BACK = 3, F_P = 4, F_F = 5, F_FLAG = 6,
@@ -107,6 +108,24 @@ float ref_residual(const float *p, const float *f, const float *flag, float *r, 
   float l2 = calculateResidualField(P, F, FL, R, hh);
   std::memcpy(r, R.data(), n * 4);
   return l2;
+}
+
+// bilinearSample / bilinearScatter (interpolators.hpp:11-40) over n points,
+// the scatter sequential in item order, on a copy of a w x h grid.
+void ref_bilinear_sample_n(const float *grid, int w, int h, int n, const float *xy, float *out) {
+  Single2DGrid G(w, h);
+  std::memcpy(G.data(), grid, (size_t)w * h * 4);
+  for (int i = 0; i < n; i++) out[i] = bilinearSample(G, glm::vec2(xy[2 * i], xy[2 * i + 1]));
+}
+void ref_bilinear_scatter_n(float *grid, int w, int h, int n, const float *xy, const float *v) {
+  Single2DGrid G(w, h);
+  std::memcpy(G.data(), grid, (size_t)w * h * 4);
+  for (int i = 0; i < n; i++) bilinearScatter(G, glm::vec2(xy[2 * i], xy[2 * i + 1]), v[i]);
+  std::memcpy(grid, G.data(), (size_t)w * h * 4);
+}
+// Simulation::setGrids (simulation.hpp:82-98).
+void ref_set_grids(void *sp, int x, int y, float val) {
+  static_cast<Simulation *>(sp)->setGrids(glm::ivec2(x, y), val);
 }
 
 }  // extern "C"

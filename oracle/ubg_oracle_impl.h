@@ -549,8 +549,16 @@ void FN(advect)(SIM_T *s) {
 
 /* -------------------------------------------------------------- projection */
 /* project, simulation.cpp:164-208: divergence into f, explosion sinks, two
- * MG V-cycles, setPBC, pressure-gradient update of the interior faces. */
-void FN(project_ncycles)(SIM_T *s, int ncycles) {
+ * MG V-cycles, setPBC, pressure-gradient update of the interior faces.
+ * Options of the extension solvers:
+ *  meanfree: the solver's system has zero-gradient edges everywhere, so it
+ *    is singular and only the part of f orthogonal to the constants is
+ *    solvable; the mean of f over the interior fluid cells (sum in double)
+ *    is subtracted from those cells before the V-cycles (tolerance modes);
+ *  zgbc_first: the zero-gradient edges are applied to p before the first
+ *    V-cycle, which makes k V-cycles equal (in exact arithmetic) to the
+ *    mixed-precision solver's k defect corrections. */
+void FN(project_opts)(SIM_T *s, int ncycles, int meanfree, int zgbc_first) {
   int W = s->W, H = s->H;
   REAL ih = (REAL)1.0 / s->h;
   REAL *vx = s->vxb[s->fx], *vy = s->vyb[s->fy];
@@ -583,6 +591,20 @@ void FN(project_ncycles)(SIM_T *s, int ncycles) {
     }
   }
   s->nsinks = keep;
+  if (meanfree) {
+    double sum = 0.0, n = 0.0;
+    for (y = 1; y < H - 1; y++)
+      for (int x = 1; x < W - 1; x++)
+        if (AT(flag, W, x, y) != (REAL)0) {
+          sum += (double)AT(s->f, W, x, y);
+          n += 1.0;
+        }
+    REAL mean = n > 0.0 ? (REAL)(sum / n) : (REAL)0;
+    for (y = 1; y < H - 1; y++)
+      for (int x = 1; x < W - 1; x++)
+        if (AT(flag, W, x, y) != (REAL)0) AT(s->f, W, x, y) -= mean;
+  }
+  if (zgbc_first) FN(zero_gradient_bc)(s->p, W, H);
   for (int c = 0; c < ncycles; c++) FN(mg_solve)(&s->mg, s->p, s->f, flag, s->h, 1);
   FN(set_pbc)(s);
 #pragma omp parallel for schedule(static)
@@ -597,6 +619,7 @@ void FN(project_ncycles)(SIM_T *s, int ncycles) {
                            (AT(s->p, W, x, y + 1) - AT(s->p, W, x, y));
 }
 
+void FN(project_ncycles)(SIM_T *s, int ncycles) { FN(project_opts)(s, ncycles, 0, 0); }
 void FN(project)(SIM_T *s) { FN(project_ncycles)(s, 2); }
 
 /* applyAccumulatedVelocity, simulation.cpp:376-396. */

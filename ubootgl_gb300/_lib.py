@@ -45,6 +45,14 @@ _SIGS = {
     "ubg_step": (C.c_int, [_P, C.c_float]),
     "ubg_step_cfl": (C.c_int, [_P, C.c_float]),
     "ubg_last_dt": (C.c_int, [_P, _FP]),
+    "ubg_solver_stats": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "ubg_scatter_accum": (C.c_int, [_P, C.c_int, _FP, _FP]),
+    "ubg_sample_velocity": (C.c_int, [_P, C.c_int, _FP, _FP]),
+    "ubg_set_grids": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), _FP]),
+    "ubg_shift_map": (C.c_int, [_P, _FP]),
+    "ubg_snapshot_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
+    "ubg_snapshot": (C.c_int, [_P, C.c_void_p]),
+    "ubg_restore": (C.c_int, [_P, C.c_void_p]),
     "ubg_apply_accumulated_velocity": (C.c_int, [_P]),
     "ubg_diffuse": (C.c_int, [_P, C.c_float]),
     "ubg_advect": (C.c_int, [_P, C.c_float]),

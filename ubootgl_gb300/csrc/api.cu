@@ -9,7 +9,9 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
+#include <algorithm>
 
 #include "ubg_internal.cuh"
 
@@ -93,6 +95,7 @@ struct ubg_sim {
   float *ax = nullptr, *ay = nullptr;
   uint8_t *codes_x = nullptr, *codes_y = nullptr;
   MgHier mg;
+  MgLow lo;  // 16-bit correction hierarchy of the mixed-precision modes
   StepScalars *d_sc = nullptr;
   unsigned int *d_umax = nullptr;
   SinkCell *d_sinks = nullptr;
@@ -109,6 +112,7 @@ struct ubg_sim {
   bool umax_ready = false;  // d_umax holds max|u| of the current fields
   float last_dt = 0.0f;
   int last_vcycles = 0;
+  double last_rel = -1.0;  // ||r|| / ||f|| after the last tolerance-mode solve
   // CUDA graph of the fixed-cycle step body
   cudaGraphExec_t graph = nullptr;
   int graph_key = -1;
@@ -119,6 +123,33 @@ struct ubg_sim {
   long launches_last = 0;
   double step_ms_total = 0.0;
   long steps_profiled = 0;
+  // grow-only device scratch for the item / cell lists of the game-side calls
+  void *scratch = nullptr;
+  size_t scratch_bytes = 0;
+
+  void *scratch_get(size_t bytes) {
+    if (bytes > scratch_bytes) {
+      sync();
+      if (scratch) cudaFree(scratch);
+      scratch = nullptr;
+      scratch_bytes = 0;
+      size_t b = std::max(bytes, (size_t)1 << 16);
+      if (cudaMalloc(&scratch, b) != cudaSuccess) {
+        cudaGetLastError();
+        throw std::bad_alloc();
+      }
+      scratch_bytes = b;
+    }
+    return scratch;
+  }
+
+  // The flag changed on the device: coarse flags and every stencil code
+  // (MG::updateFields on the device flag, plus the face codes).
+  void flag_changed() {
+    mg_update_fields(mg, st);
+    launch_face_codes(v, flag(), codes_x, codes_y, st);
+    umax_ready = false;
+  }
 
   ~ubg_sim() {
     if (st) cudaStreamSynchronize(st);
@@ -130,6 +161,8 @@ struct ubg_sim {
     if (h_ring) cudaFreeHost(h_ring);
     if (h_sinks) cudaFreeHost(h_sinks);
     if (h_norm) cudaFreeHost(h_norm);
+    mg_low_free(lo);
+    if (scratch) cudaFree(scratch);
     mg_free(mg);
     if (arena) cudaFree(arena);
     if (st) cudaStreamDestroy(st);
@@ -201,20 +234,42 @@ struct ubg_sim {
   }
 
   void solve_pressure() {
+    if (opt.precision != UBG_FP32) {
+      solve_mixed();
+      return;
+    }
     if (opt.solver_mode == UBG_SOLVE_TOLERANCE) {
       solve_tolerance();
       return;
     }
     for (int c = 0; c < opt.vcycles; c++) mg_solve(mg, true, st);
     last_vcycles = opt.vcycles;
+    last_rel = -1.0;
   }
 
-  // Extension: V-cycles until ||r|| <= tol * ||f|| (FP64 norms).
+  // Extension: FP32 defect correction around a 16-bit V-cycle.  Fixed mode:
+  // `vcycles` corrections (no host synchronisation, capturable), equal in
+  // exact arithmetic to `vcycles` V-cycles started from p with zero-gradient
+  // edges.  Tolerance mode: on the compatible system (mean-free f).
+  void solve_mixed() {
+    if (lo.levels != mg.levels || lo.prec != opt.precision)
+      throw std::runtime_error("mixed-precision hierarchy not allocated (ubg_set_options)");
+    if (opt.solver_mode == UBG_SOLVE_TOLERANCE) {
+      double fnorm2 = mg_meanfree_rhs(mg, st, true);
+      last_vcycles = mg_solve_mixed(mg, lo, opt.tol, opt.max_vcycles, fnorm2, &last_rel, st);
+    } else {
+      last_vcycles = mg_solve_mixed(mg, lo, 0.0, opt.vcycles, 0.0, nullptr, st);
+      last_rel = -1.0;
+    }
+  }
+
+  // Extension: V-cycles until ||r|| <= tol * ||f|| (FP64 norms) on the
+  // compatible part of the system (f minus its mean over the interior fluid
+  // cells; the zero-gradient system is singular).
   void solve_tolerance() {
     MgLevel &L0 = mg.lv[0];
     int c = 0;
-    double fnorm2 = 0.0;
-    level_residual_of_rhs(L0, &fnorm2);
+    double fnorm2 = mg_meanfree_rhs(mg, st, true);
     double target2 = (double)opt.tol * (double)opt.tol * fnorm2;
     for (c = 0; c < opt.max_vcycles; c++) {
       // the level-0 post-smoothing launch returns ||r||^2 of its result
@@ -231,18 +286,7 @@ struct ubg_sim {
       }
     }
     last_vcycles = c;
-  }
-
-  void level_residual_of_rhs(MgLevel &L0, double *out) {
-    // ||f * flag|| is the residual of p = 0: run the residual kernel on the
-    // idle ping-pong buffer after zeroing it.
-    float *zero = L0.e[1 - mg.cur0];
-    UBG_CUDA(cudaMemsetAsync(zero, 0, sizeof(float) * (size_t)L0.pitch * L0.h, st));
-    UBG_CUDA(cudaMemsetAsync(mg.norm, 0, sizeof(double), st));
-    level_residual(L0, 1 - mg.cur0, nullptr, mg.norm, st);
-    UBG_CUDA(cudaMemcpyAsync(h_norm, mg.norm, sizeof(double), cudaMemcpyDeviceToHost, st));
-    UBG_CUDA(cudaStreamSynchronize(st));
-    *out = *h_norm;
+    last_rel = std::sqrt(*h_norm / (fnorm2 > 0.0 ? fnorm2 : 1.0));
   }
 
   // project(), simulation.cpp:164-208 (without the trailing setVBCs of step).
@@ -291,7 +335,7 @@ struct ubg_sim {
     bool graphable = opt.use_graph && opt.solver_mode == UBG_SOLVE_FIXED && nsc == 0 && !prof;
     if (graphable) {
       // The body only depends on (fx, fy, cur0) parity and the cycle count.
-      int key = (fx << 2) | (fy << 1) | mg.cur0 | (opt.vcycles << 3);
+      int key = (fx << 2) | (fy << 1) | mg.cur0 | (opt.vcycles << 3) | (opt.precision << 24);
       if (!graph || graph_key != key) capture(key);
       UBG_CUDA(cudaGraphLaunch(graph, st));
       // replay the index bookkeeping of the captured body
@@ -529,7 +573,15 @@ int ubg_set_options(ubg_sim *s, const ubg_options *o) {
       throw ArgError("solver_mode");
     if (o->vcycles < 0 || o->vcycles > 1000) throw ArgError("vcycles out of range");
     if (o->max_vcycles < 1 || o->max_vcycles > 100000) throw ArgError("max_vcycles out of range");
-    if (o->precision != UBG_FP32) throw ArgError("precision mode not available on a simulation handle");
+    if (o->precision != UBG_FP32 && o->precision != UBG_MIXED_FP16 &&
+        o->precision != UBG_MIXED_BF16)
+      throw ArgError("precision");
+    if (o->solver_mode == UBG_SOLVE_TOLERANCE && !(o->tol > 0.0f)) throw ArgError("tol must be > 0");
+    UBG_CUDA(cudaStreamSynchronize(s->st));
+    if (o->precision == UBG_FP32)
+      mg_low_free(s->lo);
+    else if (s->lo.prec != o->precision || s->lo.levels != s->mg.levels)
+      mg_low_alloc(s->lo, s->mg, o->precision);
     s->opt = *o;
     s->graph_key = -1;
     return UBG_OK;
@@ -560,6 +612,15 @@ int ubg_step_cfl(ubg_sim *s, float cfl) {
     if (!s) throw ArgError("null handle");
     if (!s->sinks.empty()) throw ArgError("sinks need a host dt (use ubg_step)");
     s->step(0.0f, true, cfl);
+    return UBG_OK;
+  });
+}
+
+int ubg_solver_stats(ubg_sim *s, int *vcycles, double *rel_residual) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    if (vcycles) *vcycles = s->last_vcycles;
+    if (rel_residual) *rel_residual = s->last_rel;
     return UBG_OK;
   });
 }
@@ -1085,3 +1146,208 @@ int ubg_residual(const float *p, const float *f, const float *flag, float *r, in
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ game-side field access
+
+int ubg_scatter_accum(ubg_sim *s, int n, const float *xy, const float *v) {
+  return guarded([&] {
+    if (!s || n < 0 || (n > 0 && (!xy || !v))) throw ArgError("null argument");
+    if (n == 0) return UBG_OK;
+    size_t b = (size_t)n * sizeof(float2);
+    char *d = (char *)s->scratch_get(2 * b);
+    UBG_CUDA(cudaMemcpyAsync(d, xy, b, cudaMemcpyHostToDevice, s->st));
+    UBG_CUDA(cudaMemcpyAsync(d + b, v, b, cudaMemcpyHostToDevice, s->st));
+    launch_scatter_accum(s->ax, s->ay, s->P, s->W, s->H, (const float2 *)d,
+                         (const float2 *)(d + b), n, s->st);
+    s->accum_dirty = true;
+    s->sync();
+    return UBG_OK;
+  });
+}
+
+int ubg_sample_velocity(ubg_sim *s, int n, const float *xy, float *out) {
+  return guarded([&] {
+    if (!s || n < 0 || (n > 0 && (!xy || !out))) throw ArgError("null argument");
+    if (n == 0) return UBG_OK;
+    size_t b = (size_t)n * sizeof(float2);
+    char *d = (char *)s->scratch_get(2 * b);
+    UBG_CUDA(cudaMemcpyAsync(d, xy, b, cudaMemcpyHostToDevice, s->st));
+    launch_sample_velocity(s->v.vx[s->fx], s->v.vy[s->fy], s->P, s->W, s->H, (const float2 *)d,
+                           (float2 *)(d + b), n, s->st);
+    UBG_CUDA(cudaMemcpyAsync(out, d + b, b, cudaMemcpyDeviceToHost, s->st));
+    s->sync();
+    return UBG_OK;
+  });
+}
+
+int ubg_set_grids(ubg_sim *s, int n, const int *xy, const float *vals) {
+  return guarded([&] {
+    if (!s || n < 0 || (n > 0 && (!xy || !vals))) throw ArgError("null argument");
+    if (n == 0) return UBG_OK;
+    // In call order: the last value of a cell wins; a cell set to 0 at any
+    // point has its faces and p zeroed.  Cells outside the grid are ignored
+    // (the reference's bounds test).
+    std::vector<int> slot((size_t)0);
+    std::vector<int2> cells;
+    std::vector<uint8_t> val, zero;
+    std::unordered_map<long long, int> at;
+    for (int i = 0; i < n; i++) {
+      int x = xy[2 * i], y = xy[2 * i + 1];
+      float f = vals[i];
+      if (!(x >= 0 && y >= 0 && x < s->W && y < s->H)) continue;
+      if (f != 0.0f && f != 1.0f) throw ArgError("flag values must be exactly 0.0 or 1.0");
+      long long key = (long long)y * s->W + x;
+      auto it = at.find(key);
+      int k;
+      if (it == at.end()) {
+        k = (int)cells.size();
+        at.emplace(key, k);
+        cells.push_back(make_int2(x, y));
+        val.push_back(0);
+        zero.push_back(0);
+      } else {
+        k = it->second;
+      }
+      val[k] = f != 0.0f;
+      if (f == 0.0f) zero[k] = 1;
+      s->flag_host[(size_t)key] = f;
+    }
+    int m = (int)cells.size();
+    if (m == 0) return UBG_OK;
+    size_t b = (size_t)m * sizeof(int2);
+    char *d = (char *)s->scratch_get(b + 2 * (size_t)m + 16);
+    UBG_CUDA(cudaMemcpyAsync(d, cells.data(), b, cudaMemcpyHostToDevice, s->st));
+    UBG_CUDA(cudaMemcpyAsync(d + b, val.data(), m, cudaMemcpyHostToDevice, s->st));
+    UBG_CUDA(cudaMemcpyAsync(d + b + m, zero.data(), m, cudaMemcpyHostToDevice, s->st));
+    launch_set_grids((const int2 *)d, (const uint8_t *)(d + b), (const uint8_t *)(d + b + m), m,
+                     s->flag(), s->v.vx[s->fx], s->v.vy[s->fy], s->p(), s->P, s->W, s->H, s->st);
+    s->flag_changed();
+    s->sync();
+    return UBG_OK;
+  });
+}
+
+int ubg_shift_map(ubg_sim *s, const float *new_flag) {
+  return guarded([&] {
+    if (!s || !new_flag) throw ArgError("null argument");
+    const int W = s->W, H = s->H;
+    std::vector<uint8_t> u8;
+    flag_to_u8(new_flag, W, H, u8, s->P);
+    // inletArea and inletVelocity in float, in the reference's order
+    float area = 1.0f;
+    for (int y = 0; y < H - 1; y++) area += new_flag[(size_t)y * W];
+    float u = 0.07f * (float)H / area;
+    MgLevel &L0 = s->mg.lv[0];
+    float *p_in = L0.e[s->mg.cur0], *p_out = L0.e[1 - s->mg.cur0];
+    UBG_CUDA(cudaMemcpyAsync(L0.flag, u8.data(), u8.size(), cudaMemcpyHostToDevice, s->st));
+    launch_shift_map(s->v, s->fx, s->fy, p_in, p_out, L0.flag, s->P, W, H, u, s->st);
+    s->mg.cur0 ^= 1;
+    s->flag_host.assign(new_flag, new_flag + (size_t)W * H);
+    s->flag_changed();
+    s->sync();
+    return UBG_OK;
+  });
+}
+
+// ----------------------------------------------------- snapshot / restore
+namespace {
+struct SnapHeader {
+  char magic[8];  // "UBGSNAP1"
+  int32_t version, width, height, nsinks;
+  float pwidth, mu, h, last_dt;
+  int32_t bc[4];
+  int32_t reserved[4];
+};
+constexpr int kSnapFields[] = {UBG_VX, UBG_VX_BACK, UBG_VY, UBG_VY_BACK, UBG_P,
+                               UBG_F,  UBG_VX_ACCUM, UBG_VY_ACCUM};
+
+size_t snap_bytes(const ubg_sim *s) {
+  size_t W = s->W, H = s->H;
+  size_t fl = 2 * ((W - 1) * H + W * (H - 1)) + 2 * W * H + ((W - 1) * H + W * (H - 1));
+  return sizeof(SnapHeader) + (size_t)kMaxSinks * 3 * sizeof(float) + fl * sizeof(float) + W * H;
+}
+}  // namespace
+
+int ubg_snapshot_bytes(ubg_sim *s, size_t *bytes) {
+  return guarded([&] {
+    if (!s || !bytes) throw ArgError("null argument");
+    *bytes = snap_bytes(s);
+    return UBG_OK;
+  });
+}
+
+int ubg_snapshot(ubg_sim *s, void *dst) {
+  return guarded([&] {
+    if (!s || !dst) throw ArgError("null argument");
+    char *o = (char *)dst;
+    SnapHeader hd{};
+    std::memcpy(hd.magic, "UBGSNAP1", 8);
+    hd.version = 1;
+    hd.width = s->W;
+    hd.height = s->H;
+    hd.nsinks = (int32_t)s->sinks.size();
+    hd.pwidth = s->pwidth;
+    hd.mu = s->mu;
+    hd.h = s->h;
+    hd.last_dt = s->last_dt;
+    hd.bc[0] = s->bc.w;
+    hd.bc[1] = s->bc.e;
+    hd.bc[2] = s->bc.n;
+    hd.bc[3] = s->bc.s;
+    std::memcpy(o, &hd, sizeof(hd));
+    o += sizeof(hd);
+    float *sk = (float *)o;
+    for (size_t i = 0; i < (size_t)kMaxSinks; i++) {
+      bool have = i < s->sinks.size();
+      sk[3 * i] = have ? s->sinks[i].x : 0.0f;
+      sk[3 * i + 1] = have ? s->sinks[i].y : 0.0f;
+      sk[3 * i + 2] = have ? s->sinks[i].z : 0.0f;
+    }
+    o += (size_t)kMaxSinks * 3 * sizeof(float);
+    for (int f : kSnapFields) {
+      FieldView fv = field_view(s, f);
+      UBG_CUDA(cudaMemcpy2DAsync(o, (size_t)fv.w * 4, fv.dev, (size_t)s->P * 4, (size_t)fv.w * 4,
+                                 fv.h, cudaMemcpyDeviceToHost, s->st));
+      o += (size_t)fv.w * fv.h * 4;
+    }
+    s->sync();
+    for (size_t i = 0; i < s->flag_host.size(); i++) o[i] = s->flag_host[i] != 0.0f ? 1 : 0;
+    return UBG_OK;
+  });
+}
+
+int ubg_restore(ubg_sim *s, const void *src) {
+  return guarded([&] {
+    if (!s || !src) throw ArgError("null argument");
+    const char *o = (const char *)src;
+    SnapHeader hd;
+    std::memcpy(&hd, o, sizeof(hd));
+    if (std::memcmp(hd.magic, "UBGSNAP1", 8) != 0 || hd.version != 1)
+      throw ArgError("not a snapshot of this format");
+    if (hd.width != s->W || hd.height != s->H) throw ArgError("snapshot grid size differs");
+    if (hd.nsinks < 0 || hd.nsinks > kMaxSinks) throw ArgError("snapshot sink count");
+    o += sizeof(hd);
+    const float *sk = (const float *)o;
+    s->sinks.clear();
+    for (int i = 0; i < hd.nsinks; i++) s->sinks.push_back(HostSink{sk[3 * i], sk[3 * i + 1], sk[3 * i + 2]});
+    o += (size_t)kMaxSinks * 3 * sizeof(float);
+    s->sync();
+    for (int f : kSnapFields) {
+      FieldView fv = field_view(s, f);
+      UBG_CUDA(cudaMemcpy2DAsync(fv.dev, (size_t)s->P * 4, o, (size_t)fv.w * 4, (size_t)fv.w * 4,
+                                 fv.h, cudaMemcpyHostToDevice, s->st));
+      o += (size_t)fv.w * fv.h * 4;
+    }
+    std::vector<float> fl((size_t)s->W * s->H);
+    for (size_t i = 0; i < fl.size(); i++) fl[i] = o[i] ? 1.0f : 0.0f;
+    upload_flag_u8(s->mg.lv[0], fl.data(), s->W, s->H, s->st);
+    s->flag_host.swap(fl);
+    s->bc = Bcs{hd.bc[0], hd.bc[1], hd.bc[2], hd.bc[3]};
+    s->last_dt = hd.last_dt;
+    s->accum_dirty = true;
+    s->graph_key = -1;
+    s->flag_changed();
+    s->sync();
+    return UBG_OK;
+  });
+}

@@ -18,10 +18,18 @@
 // all red points, then all black points, which is the reference's
 // deterministic schedule.  Every kernel reads one buffer and writes another,
 // so tiles never race on their halos.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "ubg_internal.cuh"
 
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #define ALPHA_IS_ONE(a) ((a) == 1.0f)
 
@@ -53,21 +61,23 @@ __global__ void k_make_code(const uint8_t *__restrict__ flag, uint8_t *code, int
 // at +0 and never becomes -0), val/sum is exact as a multiplication for
 // sum = 1, 2, 4 and a true division for sum = 3, and flag*val equals
 // flag ? val : 0 up to the sign of a zero.
-__device__ __forceinline__ float rb_update1(unsigned c, float pw, float pe, float ps, float pn,
-                                            float f, float hh) {
-  float val = 0.0f;
-  val = val + ((c & C_W) ? pw : 0.0f);
-  val = val + ((c & C_E) ? pe : 0.0f);
-  val = val + ((c & C_S) ? ps : 0.0f);
-  val = val + ((c & C_N) ? pn : 0.0f);
+// T = float is the reference's arithmetic; T = double serves the FP64
+// coarse solve of the mixed-precision solver.
+template <class T>
+__device__ __forceinline__ T rb_update1(unsigned c, T pw, T pe, T ps, T pn, T f, T hh) {
+  T val = T(0);
+  val = val + ((c & C_W) ? pw : T(0));
+  val = val + ((c & C_E) ? pe : T(0));
+  val = val + ((c & C_S) ? ps : T(0));
+  val = val + ((c & C_N) ? pn : T(0));
   val = val + f * hh * hh;
   int s = __popc((c >> 1) & 15u);
   if (s == 3)
-    val = val / 3.0f;
+    val = val / T(3);
   else
-    val = val * (s == 4 ? 0.25f : (s == 2 ? 0.5f : (s == 1 ? 1.0f : 0.0f)));
-  if (s == 0) val = 0.0f;
-  return (c & C_CENTER) ? val : 0.0f;
+    val = val * (s == 4 ? T(0.25) : (s == 2 ? T(0.5) : (s == 1 ? T(1) : T(0))));
+  if (s == 0) val = T(0);
+  return (c & C_CENTER) ? val : T(0);
 }
 
 // General alpha (the free function rbgs(p, f, flag, h, alpha)).
@@ -91,63 +101,132 @@ __device__ __forceinline__ float rb_update_alpha(unsigned c, float pc, float pw,
 
 // calculateResidualField at one cell (pressure_solver.cpp:100-110): a
 // neighbour term p_n*flag_n + p*(1-flag_n) is flag_n ? p_n : p.
-__device__ __forceinline__ float resid1(unsigned c, float pc, float pw, float pe, float ps,
-                                        float pn, float f, float ihsq) {
-  float val = 0.0f;
+template <class T>
+__device__ __forceinline__ T resid1(unsigned c, T pc, T pw, T pe, T ps, T pn, T f, T ihsq) {
+  T val = T(0);
   val = val + ((c & C_W) ? pw : pc);
   val = val + ((c & C_E) ? pe : pc);
   val = val + ((c & C_S) ? ps : pc);
   val = val + ((c & C_N) ? pn : pc);
-  val = val + -4.0f * pc;
+  val = val + T(-4) * pc;
   val = val * ihsq;
-  return (c & C_CENTER) ? (f + val) : 0.0f;
+  return (c & C_CENTER) ? (f + val) : T(0);
 }
 
-struct MgArgs {
-  const float *in;
-  float *out;
-  const float *rhs;
+// Storage of the smoothed arrays: float (the reference's arithmetic, and the
+// only type whose results are compared bit for bit) or __half /
+// __nv_bfloat16 for the low-precision correction V-cycle of the mixed
+// solver.  Arithmetic is always FP32 in registers.
+template <class S>
+struct Sto;
+template <>
+struct Sto<float> {
+  static __device__ __forceinline__ float4 ldg4(const float *p) {
+    return __ldg(reinterpret_cast<const float4 *>(p));
+  }
+  static __device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+  static __device__ __forceinline__ float4 lds4(const float *p) {
+    return *reinterpret_cast<const float4 *>(p);
+  }
+  static __device__ __forceinline__ void sts4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+  static __device__ __forceinline__ float2 lds2(const float *p) {
+    return *reinterpret_cast<const float2 *>(p);
+  }
+  static __device__ __forceinline__ void sts2(float *p, float a, float b) {
+    *reinterpret_cast<float2 *>(p) = make_float2(a, b);
+  }
+  static __device__ __forceinline__ float tof(float v) { return v; }
+  static __device__ __forceinline__ float fromf(float v) { return v; }
+  static __device__ __forceinline__ float ldg1(const float *p) { return __ldg(p); }
+};
+template <>
+struct Sto<__half> {
+  static __device__ __forceinline__ float4 unpack(uint2 u) {
+    float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+    float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+  }
+  static __device__ __forceinline__ uint2 pack(float4 v) {
+    __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+    return make_uint2(*reinterpret_cast<unsigned *>(&a), *reinterpret_cast<unsigned *>(&b));
+  }
+  static __device__ __forceinline__ float4 ldg4(const __half *p) {
+    return unpack(__ldg(reinterpret_cast<const uint2 *>(p)));
+  }
+  static __device__ __forceinline__ void st4(__half *p, float4 v) { *reinterpret_cast<uint2 *>(p) = pack(v); }
+  static __device__ __forceinline__ float4 lds4(const __half *p) {
+    return unpack(*reinterpret_cast<const uint2 *>(p));
+  }
+  static __device__ __forceinline__ void sts4(__half *p, float4 v) { *reinterpret_cast<uint2 *>(p) = pack(v); }
+  static __device__ __forceinline__ float2 lds2(const __half *p) {
+    return __half22float2(*reinterpret_cast<const __half2 *>(p));
+  }
+  static __device__ __forceinline__ void sts2(__half *p, float a, float b) {
+    *reinterpret_cast<__half2 *>(p) = __floats2half2_rn(a, b);
+  }
+  static __device__ __forceinline__ float tof(__half v) { return __half2float(v); }
+  static __device__ __forceinline__ __half fromf(float v) { return __float2half_rn(v); }
+  static __device__ __forceinline__ float ldg1(const __half *p) { return __half2float(__ldg(p)); }
+};
+template <>
+struct Sto<__nv_bfloat16> {
+  static __device__ __forceinline__ float4 unpack(uint2 u) {
+    float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.x));
+    float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+  }
+  static __device__ __forceinline__ uint2 pack(float4 v) {
+    __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
+    return make_uint2(*reinterpret_cast<unsigned *>(&a), *reinterpret_cast<unsigned *>(&b));
+  }
+  static __device__ __forceinline__ float4 ldg4(const __nv_bfloat16 *p) {
+    return unpack(__ldg(reinterpret_cast<const uint2 *>(p)));
+  }
+  static __device__ __forceinline__ void st4(__nv_bfloat16 *p, float4 v) {
+    *reinterpret_cast<uint2 *>(p) = pack(v);
+  }
+  static __device__ __forceinline__ float4 lds4(const __nv_bfloat16 *p) {
+    return unpack(*reinterpret_cast<const uint2 *>(p));
+  }
+  static __device__ __forceinline__ void sts4(__nv_bfloat16 *p, float4 v) {
+    *reinterpret_cast<uint2 *>(p) = pack(v);
+  }
+  static __device__ __forceinline__ float2 lds2(const __nv_bfloat16 *p) {
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(p));
+  }
+  static __device__ __forceinline__ void sts2(__nv_bfloat16 *p, float a, float b) {
+    *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(a, b);
+  }
+  static __device__ __forceinline__ float tof(__nv_bfloat16 v) { return __bfloat162float(v); }
+  static __device__ __forceinline__ __nv_bfloat16 fromf(float v) { return __float2bfloat16_rn(v); }
+  static __device__ __forceinline__ float ldg1(const __nv_bfloat16 *p) {
+    return __bfloat162float(__ldg(p));
+  }
+};
+
+template <class S>
+struct MgArgsT {
+  const S *in;
+  S *out;
+  const S *rhs;
   const uint8_t *code;
   int w, h, pitch;
   float hh, alpha, ihsq;
   int nsweeps, zgbc, zero_init;
   // prologue: p += prolongate(ec) (post-smoothing)
-  const float *ec;
+  const S *ec;
   const uint8_t *codec;
   int cpitch;
   float wsum[5];  // (float)((double)k + 0.0001)
   // epilogue: rc = restrict(residual) (pre-smoothing)
-  float *rc;
+  S *rc;
   int cw, ch;
+  float rfac;  // restriction weight: 1/16 (reference), 1/16 * (hc/h)^2 (scaled form)
+  int tile;    // smoother tile id (-1: by level width), host side only
   // epilogue: sum of r^2 over the tile's interior cells
   double *norm2;
 };
-
-// prolongate (pressure_solver.cpp:134-172) at one fine interior cell whose
-// own flag is set.
-__device__ __forceinline__ float prolong_at(const MgArgs &a, int gx, int gy) {
-  int cx = gx >> 1, cy = gy >> 1;
-  const float *ec = a.ec;
-  const uint8_t *fc = a.codec;
-  int cp = a.cpitch;
-  auto E = [&](int x, int y) { return __ldg(ec + (size_t)y * cp + x); };
-  auto F = [&](int x, int y) { return (int)(__ldg(fc + (size_t)y * cp + x) & 1u); };
-  bool xo = gx & 1, yo = gy & 1;
-  if (!xo && !yo) return E(cx, cy);
-  if (xo && !yo) {
-    if (gx >= a.w - 2) return 0.0f;
-    float sum = a.wsum[F(cx, cy) + F(cx + 1, cy)];
-    return (E(cx, cy) + E(cx + 1, cy)) / sum;
-  }
-  if (!xo && yo) {
-    if (gy >= a.h - 2) return 0.0f;
-    float sum = a.wsum[F(cx, cy) + F(cx, cy + 1)];
-    return (E(cx, cy) + E(cx, cy + 1)) / sum;
-  }
-  if (gx >= a.w - 2 || gy >= a.h - 2) return 0.0f;
-  float sum = a.wsum[F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1)];
-  return (((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1)) / sum;
-}
+using MgArgs = MgArgsT<float>;
 
 template <int TX, int TY, int HALO>
 struct Tile {
@@ -155,8 +234,11 @@ struct Tile {
   // coarse window for the prolongation prologue
   static constexpr int CW = HX + 2, CH = RY / 2 + 2;
   static_assert(RX % 4 == 0 && HALO % 4 == 0 && TX % 4 == 0 && TY % 2 == 0, "tile alignment");
-  static constexpr size_t smem() {
-    return (size_t)2 * RY * HX * (4 + 4 + 1) + (size_t)CW * CH * 4 + ((size_t)CW * CH + 15) / 16 * 16;
+  // shared memory for element size ES: p and f in the split layout, codes,
+  // the coarse window (values and flags)
+  static constexpr size_t smem(size_t ES = 4) {
+    return (size_t)2 * RY * HX * (2 * ES + 1) + (((size_t)CW * CH * ES + 15) / 16 * 16) +
+           ((size_t)CW * CH + 15) / 16 * 16;
   }
 };
 
@@ -167,14 +249,15 @@ struct Tile {
 // (no bank conflicts).  Red = (x+y) odd; region parity equals global parity
 // because x0 + y0 is even.  After half sweep i only cells within HALO - i of
 // the tile are still exact, so each half sweep updates just that cone.
-template <int TX, int TY, int HALO, bool ALPHA1, int NT>
-__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
+template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgsT<S> a) {
   constexpr int NTY = NT / 32;
   using T = Tile<TX, TY, HALO>;
+  using St = Sto<S>;
   constexpr int RX = T::RX, RY = T::RY, HX = T::HX;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *sp = reinterpret_cast<float *>(smem_raw);  // [2][RY][HX]
-  float *sf = sp + 2 * RY * HX;
+  S *sp = reinterpret_cast<S *>(smem_raw);  // [2][RY][HX]
+  S *sf = sp + 2 * RY * HX;
   uint8_t *sc = reinterpret_cast<uint8_t *>(sf + 2 * RY * HX);
   auto IDX = [](int rx, int ry) { return (((rx + ry) & 1) * RY + ry) * HX + (rx >> 1); };
 
@@ -186,7 +269,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
   // One array at a time, all of a thread's loads of that array in flight
   // together, into the red/black-split layout.
   constexpr int NQ = RY * (RX / 4), NIT = (NQ + NT - 1) / NT;
-  auto load_split = [&](const float *src, float *dst, bool zero) {
+  auto load_split = [&](const S *src, S *dst, bool zero) {
     float4 v[NIT];
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
@@ -195,7 +278,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
       int gx = x0 + 4 * g, gy = y0 + ry;
       v[it] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (!zero && q < NQ && gy >= 0 && gy < h && gx >= 0 && gx < w)
-        v[it] = __ldg(reinterpret_cast<const float4 *>(src + (size_t)gy * P + gx));
+        v[it] = St::ldg4(src + (size_t)gy * P + gx);
     }
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
@@ -210,8 +293,8 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
         p4.w = 0.f;
       }
       int c0 = ry & 1;
-      *reinterpret_cast<float2 *>(dst + (c0 * RY + ry) * HX + 2 * g) = make_float2(p4.x, p4.z);
-      *reinterpret_cast<float2 *>(dst + ((c0 ^ 1) * RY + ry) * HX + 2 * g) = make_float2(p4.y, p4.w);
+      St::sts2(dst + (c0 * RY + ry) * HX + 2 * g, p4.x, p4.z);
+      St::sts2(dst + ((c0 ^ 1) * RY + ry) * HX + 2 * g, p4.y, p4.w);
     }
   };
   load_split(a.in, sp, a.zero_init != 0);
@@ -253,8 +336,9 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
   // the coarse window staged in shared memory
   if (a.ec) {
     constexpr int CW = T::CW, CH = T::CH;
-    float *sec = reinterpret_cast<float *>(sc + 2 * RY * HX);
-    uint8_t *scf = reinterpret_cast<uint8_t *>(sec + CW * CH);
+    S *sec = reinterpret_cast<S *>(sc + 2 * RY * HX);
+    uint8_t *scf = reinterpret_cast<uint8_t *>(sc + 2 * RY * HX) +
+                   ((size_t)CW * CH * sizeof(S) + 15) / 16 * 16;
     const int cxa = x0 >> 1, cya = y0 >> 1;
     for (int q = tid; q < CW * CH; q += NT) {
       int ly = q / CW, lx = q - ly * CW;
@@ -262,10 +346,10 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
       float e = 0.0f;
       uint8_t fc = 0;
       if (cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
-        e = __ldg(a.ec + (size_t)cy * a.cpitch + cx);
+        e = St::ldg1(a.ec + (size_t)cy * a.cpitch + cx);
         fc = __ldg(a.codec + (size_t)cy * a.cpitch + cx) & 1u;
       }
-      sec[q] = e;
+      sec[q] = St::fromf(e);
       scf[q] = fc;
     }
     __syncthreads();
@@ -280,22 +364,23 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
           int i = (color * RY + ry) * HX + k;
           if (gx < 1 || gx >= w - 1 || !(sc[i] & C_CENTER)) continue;
           // prolongate (pressure_solver.cpp:134-172); e * fine flag = e here
-          const float *E = sec + (ry >> 1) * CW + (rx >> 1);
+          const S *Es = sec + (ry >> 1) * CW + (rx >> 1);
           const uint8_t *F = scf + (ry >> 1) * CW + (rx >> 1);
+          auto E = [&](int o) { return St::tof(Es[o]); };
           bool xo = gx & 1, yo = gy & 1;
           float ev;
           if (!xo && !yo) {
-            ev = E[0];
+            ev = E(0);
           } else if (xo && !yo) {
-            ev = (gx >= w - 2) ? 0.0f : (E[0] + E[1]) / a.wsum[F[0] + F[1]];
+            ev = (gx >= w - 2) ? 0.0f : (E(0) + E(1)) / a.wsum[F[0] + F[1]];
           } else if (!xo && yo) {
-            ev = (gy >= h - 2) ? 0.0f : (E[0] + E[CW]) / a.wsum[F[0] + F[CW]];
+            ev = (gy >= h - 2) ? 0.0f : (E(0) + E(CW)) / a.wsum[F[0] + F[CW]];
           } else {
             ev = (gx >= w - 2 || gy >= h - 2)
                      ? 0.0f
-                     : (((E[0] + E[CW + 1]) + E[1]) + E[CW]) / a.wsum[F[0] + F[CW + 1] + F[1] + F[CW]];
+                     : (((E(0) + E(CW + 1)) + E(1)) + E(CW)) / a.wsum[F[0] + F[CW + 1] + F[1] + F[CW]];
           }
-          sp[i] = sp[i] + ev;
+          sp[i] = St::fromf(St::tof(sp[i]) + ev);
         }
       }
     }
@@ -351,20 +436,20 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
 #pragma unroll
     for (int color = 1; color >= 0; color--) {
       half++;
-      float *self = sp + color * RY * HX;
-      const float *oth = sp + (color ^ 1) * RY * HX;
-      const float *fs = sf + color * RY * HX;
+      S *self = sp + color * RY * HX;
+      const S *oth = sp + (color ^ 1) * RY * HX;
+      const S *fs = sf + color * RY * HX;
       const uint8_t *cs = sc + color * RY * HX;
       for (int ry = half + rsub; ry <= RY - 1 - half; ry += RPP) {
         const int par = (ry + color) & 1;
         const int gy = y0 + ry;
         const int row = ry * HX + k0;
-        const float4 o = *reinterpret_cast<const float4 *>(oth + row);
-        const float ex = par ? oth[row + 4] : oth[row - 1];
-        const float4 os = *reinterpret_cast<const float4 *>(oth + row - HX);
-        const float4 on = *reinterpret_cast<const float4 *>(oth + row + HX);
-        const float4 fv = *reinterpret_cast<const float4 *>(fs + row);
-        const float4 sv = *reinterpret_cast<const float4 *>(self + row);
+        const float4 o = St::lds4(oth + row);
+        const float ex = St::tof(par ? oth[row + 4] : oth[row - 1]);
+        const float4 os = St::lds4(oth + row - HX);
+        const float4 on = St::lds4(oth + row + HX);
+        const float4 fv = St::lds4(fs + row);
+        const float4 sv = St::lds4(self + row);
         const uchar4 cv = *reinterpret_cast<const uchar4 *>(cs + row);
         const float W4[4] = {par ? o.x : ex, par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z};
         const float E4[4] = {par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z, par ? ex : o.w};
@@ -392,7 +477,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
 #pragma unroll
         for (int j = 0; j < 4; j++)
           if (!cell_ok(k0 + j, par, gy)) out[j] = P4[j];
-        *reinterpret_cast<float4 *>(self + row) = make_float4(out[0], out[1], out[2], out[3]);
+        St::sts4(self + row, make_float4(out[0], out[1], out[2], out[3]));
       }
       __syncthreads();
     }
@@ -410,16 +495,16 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
     if (gy >= h || gx >= w) continue;
     int c0 = (rx + ry) & 1;
     int b0 = (c0 * RY + ry) * HX + (rx >> 1), b1 = ((c0 ^ 1) * RY + ry) * HX + (rx >> 1);
-    float2 u = *reinterpret_cast<const float2 *>(sp + b0);
-    float2 v = *reinterpret_cast<const float2 *>(sp + b1);
+    float2 u = St::lds2(sp + b0);
+    float2 v = St::lds2(sp + b1);
     float4 o = make_float4(u.x, v.x, u.y, v.y);
-    float *dst = a.out + (size_t)gy * P + gx;
+    S *dst = a.out + (size_t)gy * P + gx;
     if (gx + 3 < w) {
-      *reinterpret_cast<float4 *>(dst) = o;
+      St::st4(dst, o);
     } else {
-      dst[0] = o.x;
-      if (gx + 1 < w) dst[1] = o.y;
-      if (gx + 2 < w) dst[2] = o.z;
+      dst[0] = St::fromf(o.x);
+      if (gx + 1 < w) dst[1] = St::fromf(o.y);
+      if (gx + 2 < w) dst[2] = St::fromf(o.z);
     }
   }
 
@@ -433,20 +518,20 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
   const int rhix = a.rc ? HALO + TX : HALO + TX - 1, rhiy = a.rc ? HALO + TY : HALO + TY - 1;
 #pragma unroll
   for (int color = 0; color < 2; color++) {
-    const float *self = sp + color * RY * HX;
-    const float *oth = sp + (color ^ 1) * RY * HX;
-    float *fs = sf + color * RY * HX;
+    const S *self = sp + color * RY * HX;
+    const S *oth = sp + (color ^ 1) * RY * HX;
+    S *fs = sf + color * RY * HX;
     const uint8_t *cs = sc + color * RY * HX;
     for (int ry = rlo + rsub; ry <= rhiy; ry += RPP) {
       const int par = (ry + color) & 1;
       const int gy = y0 + ry;
       const int row = ry * HX + k0;
-      const float4 o = *reinterpret_cast<const float4 *>(oth + row);
-      const float ex = par ? oth[row + 4] : oth[row - 1];
-      const float4 os = *reinterpret_cast<const float4 *>(oth + row - HX);
-      const float4 on = *reinterpret_cast<const float4 *>(oth + row + HX);
-      const float4 fv = *reinterpret_cast<const float4 *>(fs + row);
-      const float4 sv = *reinterpret_cast<const float4 *>(self + row);
+      const float4 o = St::lds4(oth + row);
+      const float ex = St::tof(par ? oth[row + 4] : oth[row - 1]);
+      const float4 os = St::lds4(oth + row - HX);
+      const float4 on = St::lds4(oth + row + HX);
+      const float4 fv = St::lds4(fs + row);
+      const float4 sv = St::lds4(self + row);
       const uchar4 cv = *reinterpret_cast<const uchar4 *>(cs + row);
       const float W4[4] = {par ? o.x : ex, par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z};
       const float E4[4] = {par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z, par ? ex : o.w};
@@ -465,7 +550,7 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
         }
         out[j] = r;
       }
-      if (a.rc) *reinterpret_cast<float4 *>(fs + row) = make_float4(out[0], out[1], out[2], out[3]);
+      if (a.rc) St::sts4(fs + row, make_float4(out[0], out[1], out[2], out[3]));
     }
   }
   __syncthreads();
@@ -491,13 +576,13 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgs a) {
       float v = 0.0f;
       if (X >= 1 && X < a.cw - 1 && Y >= 1 && Y < a.ch - 1) {
         int rx = 2 * X - x0, ry = 2 * Y - y0;
-        auto R = [&](int dx, int dy) { return sf[IDX(rx + dx, ry + dy)]; };
+        auto R = [&](int dx, int dy) { return St::tof(sf[IDX(rx + dx, ry + dy)]); };
         v = (R(-1, -1) * 1.0f + R(0, -1) * 2.0f) + R(1, -1) * 1.0f;
         v = v + ((R(-1, 0) * 2.0f + R(0, 0) * 4.0f) + R(1, 0) * 2.0f);
         v = v + ((R(-1, 1) * 1.0f + R(0, 1) * 2.0f) + R(1, 1) * 1.0f);
-        v = v * (1.0f / 16.0f);
+        v = v * a.rfac;
       }
-      a.rc[(size_t)Y * a.cpitch + X] = v;
+      a.rc[(size_t)Y * a.cpitch + X] = St::fromf(v);
     }
   }
 }
@@ -572,19 +657,20 @@ constexpr size_t TAIL_SMEM_MAX = 160 * 1024;
 
 struct TailLevel {
   int w, h;
-  float hh, ihsq;
-  int oe, orr, orhs, oc;  // offsets: floats for e / r / rhs, bytes for code
+  float hh, ihsq, rfac;
+  int oe, orr, orhs, oc;  // offsets: elements for e / r / rhs, bytes for code
 };
+template <class S>
 struct TailArgs {
   int nlev;
   TailLevel L[TAIL_MAXL];
   const uint8_t *code[TAIL_MAXL];
   int code_pitch[TAIL_MAXL];
-  const float *rhs_top;
+  const S *rhs_top;
   int rhs_pitch;
-  float *e_top;
+  S *e_top;
   int e_pitch;
-  int float_words;  // size of the float part of shared memory
+  int float_words;  // elements of the arithmetic part of shared memory
   float wsum[5];
 };
 
@@ -600,13 +686,18 @@ __device__ __forceinline__ void team_sync(int team) {
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs a) {
+// S: storage of the top level's rhs and result (float, or the 16-bit type of
+// the mixed solver); T: arithmetic and shared-memory type (float, or double
+// for the FP64 coarse solve of the mixed solver).
+template <class S, class T>
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs<S> a) {
+  using St = Sto<S>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *fm = reinterpret_cast<float *>(smem_raw);
-  uint8_t *bm = smem_raw + (size_t)a.float_words * 4;
+  T *fm = reinterpret_cast<T *>(smem_raw);
+  uint8_t *bm = smem_raw + (size_t)a.float_words * sizeof(T);
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
   const int nl = a.nlev;
-  const float ws0 = a.wsum[0], ws1 = a.wsum[1], ws2 = a.wsum[2], ws3 = a.wsum[3], ws4 = a.wsum[4];
+  const T ws0 = a.wsum[0], ws1 = a.wsum[1], ws2 = a.wsum[2], ws3 = a.wsum[3], ws4 = a.wsum[4];
   auto WS = [&](int k) {
     return k == 0 ? ws0 : (k == 1 ? ws1 : (k == 2 ? ws2 : (k == 3 ? ws3 : ws4)));
   };
@@ -621,19 +712,19 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs a) {
       for (int x = tx; x < L.w; x += 32) {
         int q = y * L.w + x;
         bm[L.oc + q] = a.code[t][(size_t)y * a.code_pitch[t] + x];
-        fm[L.oe + q] = 0.0f;
-        if (t == 0) fm[L.orhs + q] = a.rhs_top[(size_t)y * a.rhs_pitch + x];
+        fm[L.oe + q] = T(0);
+        if (t == 0) fm[L.orhs + q] = (T)St::tof(a.rhs_top[(size_t)y * a.rhs_pitch + x]);
       }
   }
   __syncthreads();
 
   auto sweeps = [&](int t, int ns, int team) {
     const TailLevel &L = a.L[t];
-    float *e = fm + L.oe;
-    const float *f = fm + L.orhs;
+    T *e = fm + L.oe;
+    const T *f = fm + L.orhs;
     const uint8_t *c = bm + L.oc;
     const int w = L.w, hw2 = (w + 1) / 2, ystep = team / 32;
-    const float hh = L.hh;
+    const T hh = (T)L.hh;
     for (int s = 0; s < ns; s++) {
       for (int color = 1; color >= 0; color--) {
         for (int y = 1 + ty; y < L.h - 1; y += ystep) {
@@ -643,11 +734,11 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs a) {
             if (x < 1 || x >= w - 1) continue;
             int i = y * w + x;
             unsigned ci = c[i];
-            float pw = e[i - 1], pe = e[i + 1], ps = e[i - w], pn = e[i + w], fi = f[i];
+            T pw = e[i - 1], pe = e[i + 1], ps = e[i - w], pn = e[i + w], fi = f[i];
             if (__all_sync(__activemask(), ci == (C_CENTER | C_W | C_E | C_S | C_N)))
-              e[i] = ((((pw + pe) + ps) + pn) + fi * hh * hh) * 0.25f;
+              e[i] = ((((pw + pe) + ps) + pn) + fi * hh * hh) * T(0.25);
             else
-              e[i] = rb_update1(ci, pw, pe, ps, pn, fi, hh);
+              e[i] = rb_update1<T>(ci, pw, pe, ps, pn, fi, hh);
           }
         }
         team_sync(team);
@@ -666,28 +757,29 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs a) {
     }
     sweeps(t, 3, team);
     const TailLevel &L = a.L[t], &C = a.L[t + 1];
-    float *e = fm + L.oe, *r = fm + L.orr;
-    const float *f = fm + L.orhs;
+    T *e = fm + L.oe, *r = fm + L.orr;
+    const T *f = fm + L.orhs;
     const uint8_t *c = bm + L.oc;
     for (int y = ty; y < L.h; y += ystep)
       for (int x = tx; x < L.w; x += 32) {
         int q = y * L.w + x;
-        float rv = 0.0f;
+        T rv = T(0);
         if (x >= 1 && x < L.w - 1 && y >= 1 && y < L.h - 1)
-          rv = resid1(c[q], e[q], e[q - 1], e[q + 1], e[q - L.w], e[q + L.w], f[q], L.ihsq);
+          rv = resid1<T>(c[q], e[q], e[q - 1], e[q + 1], e[q - L.w], e[q + L.w], f[q], (T)L.ihsq);
         r[q] = rv;
       }
     team_sync(team);
-    float *rc = fm + C.orhs;
+    T *rc = fm + C.orhs;
+    const T rfac = (T)L.rfac;
     for (int Y = ty; Y < C.h; Y += ystep)
       for (int X = tx; X < C.w; X += 32) {
-        float v = 0.0f;
+        T v = T(0);
         if (X >= 1 && X < C.w - 1 && Y >= 1 && Y < C.h - 1) {
-          const float *R0 = r + (2 * Y) * L.w + 2 * X;
-          v = (R0[-L.w - 1] * 1.0f + R0[-L.w] * 2.0f) + R0[-L.w + 1] * 1.0f;
-          v = v + ((R0[-1] * 2.0f + R0[0] * 4.0f) + R0[1] * 2.0f);
-          v = v + ((R0[L.w - 1] * 1.0f + R0[L.w] * 2.0f) + R0[L.w + 1] * 1.0f);
-          v = v * (1.0f / 16.0f);
+          const T *R0 = r + (2 * Y) * L.w + 2 * X;
+          v = (R0[-L.w - 1] * T(1) + R0[-L.w] * T(2)) + R0[-L.w + 1] * T(1);
+          v = v + ((R0[-1] * T(2) + R0[0] * T(4)) + R0[1] * T(2));
+          v = v + ((R0[L.w - 1] * T(1) + R0[L.w] * T(2)) + R0[L.w + 1] * T(1));
+          v = v * rfac;
         }
         rc[Y * C.w + X] = v;
       }
@@ -700,8 +792,8 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs a) {
     const int ystep = team / 32;
     team_sync(team);  // the coarser level's team has finished
     const TailLevel &L = a.L[t], &C = a.L[t + 1];
-    float *e = fm + L.oe;
-    const float *ec = fm + C.oe;
+    T *e = fm + L.oe;
+    const T *ec = fm + C.oe;
     const uint8_t *c = bm + L.oc, *cc = bm + C.oc;
     for (int y = 1 + ty; y < L.h - 1; y += ystep)
       for (int x = 1 + tx; x < L.w - 1; x += 32) {
@@ -711,16 +803,16 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs a) {
         auto E = [&](int xx, int yy) { return ec[yy * C.w + xx]; };
         auto F = [&](int xx, int yy) { return (int)(cc[yy * C.w + xx] & 1u); };
         bool xo = x & 1, yo = y & 1;
-        float ev;
+        T ev;
         if (!xo && !yo)
           ev = E(cx, cy);
         else if (xo && !yo)
-          ev = (x >= L.w - 2) ? 0.0f : (E(cx, cy) + E(cx + 1, cy)) / WS(F(cx, cy) + F(cx + 1, cy));
+          ev = (x >= L.w - 2) ? T(0) : (E(cx, cy) + E(cx + 1, cy)) / WS(F(cx, cy) + F(cx + 1, cy));
         else if (!xo && yo)
-          ev = (y >= L.h - 2) ? 0.0f : (E(cx, cy) + E(cx, cy + 1)) / WS(F(cx, cy) + F(cx, cy + 1));
+          ev = (y >= L.h - 2) ? T(0) : (E(cx, cy) + E(cx, cy + 1)) / WS(F(cx, cy) + F(cx, cy + 1));
         else
           ev = (x >= L.w - 2 || y >= L.h - 2)
-                   ? 0.0f
+                   ? T(0)
                    : (((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1)) /
                          WS(F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1));
         e[q] = e[q] + ev;
@@ -731,55 +823,101 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs a) {
   __syncthreads();
   const TailLevel &L0 = a.L[0];
   for (int y = ty; y < L0.h; y += 32)
-    for (int x = tx; x < L0.w; x += 32) a.e_top[(size_t)y * a.e_pitch + x] = fm[L0.oe + y * L0.w + x];
+    for (int x = tx; x < L0.w; x += 32)
+      a.e_top[(size_t)y * a.e_pitch + x] = St::fromf((float)fm[L0.oe + y * L0.w + x]);
 }
 
 // ------------------------------------------------------------ launches
-template <int TX, int TY, int HALO, bool A1, int NT = 256>
-void launch_mg_t(const MgArgs &a, cudaStream_t st) {
+template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float>
+void launch_mg_t(const MgArgsT<S> &a, cudaStream_t st) {
   using T = Tile<TX, TY, HALO>;
   dim3 grid((a.w + TX - 1) / TX, (a.h + TY - 1) / TY);
-  k_mg<TX, TY, HALO, A1, NT><<<grid, dim3(32, NT / 32), T::smem(), st>>>(a);
+  k_mg<TX, TY, HALO, A1, NT, S><<<grid, dim3(32, NT / 32), T::smem(sizeof(S)), st>>>(a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
 
-template <int TX, int TY, int HALO, bool A1, int NT = 256>
+template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float>
 void set_smem_attr() {
-  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)Tile<TX, TY, HALO>::smem()));
+  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)Tile<TX, TY, HALO>::smem(sizeof(S))));
   // one carveout for every kernel of a V-cycle: no L1 / shared-memory
   // reconfiguration between consecutive launches
-  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT>,
+  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S>,
                                 cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+}
+
+template <class S, class T>
+void set_tail_attr() {
+  UBG_CUDA(cudaFuncSetAttribute(k_mg_tail<S, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TAIL_SMEM_MAX));
+  UBG_CUDA(cudaFuncSetAttribute(k_mg_tail<S, T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+}
+
+template <class S>
+void set_vcycle_attrs() {
+  set_smem_attr<112, 50, 8, true, 512, S>();
+  set_smem_attr<48, 16, 8, true, 256, S>();
+  set_smem_attr<40, 8, 12, true, 256, S>();
+  set_smem_attr<112, 24, 8, true, 256, S>();
+  set_smem_attr<48, 40, 8, true, 256, S>();
 }
 
 void init_kernel_attributes() {
   static bool done = false;
   if (done) return;
-  set_smem_attr<112, 50, 8, true, 512>();
-  set_smem_attr<48, 16, 8, true>();
-  set_smem_attr<40, 8, 12, true>();
+  set_vcycle_attrs<float>();
   set_smem_attr<56, 24, 4, false>();
-  UBG_CUDA(cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)TAIL_SMEM_MAX));
-  UBG_CUDA(cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  set_tail_attr<float, float>();
+  set_vcycle_attrs<__half>();
+  set_vcycle_attrs<__nv_bfloat16>();
+  set_tail_attr<__half, double>();
+  set_tail_attr<__nv_bfloat16, double>();
   done = true;
 }
 
 // 3 sweeps with an optional restriction epilogue need HALO >= 8; the tile
 // is chosen by level width so small levels still fill the GPU.
-void launch_mg(const MgArgs &a, cudaStream_t st) {
+// Smoother tiles the autotuner chooses from (3-sweep launches need a halo of
+// 8, 5-sweep launches 12): id -> TX x TY, halo, threads.
+constexpr int kTiles = 5;
+const char *const kTileNames[kTiles] = {"112x50/h8/512", "48x16/h8/256", "40x8/h12/256",
+                                        "112x24/h8/256", "48x40/h8/256"};
+bool tile_ok(int id, int nsweeps) { return id >= 0 && id < kTiles && (nsweeps <= 3 || id == 2); }
+
+template <class S>
+void launch_mg_tile(const MgArgsT<S> &a, int id, cudaStream_t st) {
+  switch (id) {
+    case 0: launch_mg_t<112, 50, 8, true, 512, S>(a, st); break;
+    case 1: launch_mg_t<48, 16, 8, true, 256, S>(a, st); break;
+    case 2: launch_mg_t<40, 8, 12, true, 256, S>(a, st); break;
+    case 3: launch_mg_t<112, 24, 8, true, 256, S>(a, st); break;
+    case 4: launch_mg_t<48, 40, 8, true, 256, S>(a, st); break;
+    default: throw ArgError("smoother tile id");
+  }
+}
+
+template <class S>
+void launch_mg(const MgArgsT<S> &a, cudaStream_t st) {
+  if (ALPHA_IS_ONE(a.alpha) && a.nsweeps > 1 && a.nsweeps <= 5 && tile_ok(a.tile, a.nsweeps)) {
+    launch_mg_tile(a, a.tile, st);
+    return;
+  }
   if (!ALPHA_IS_ONE(a.alpha) || a.nsweeps == 1) {
-    if (a.nsweeps != 1) throw ArgError("general alpha: one sweep per launch");
-    launch_mg_t<56, 24, 4, false>(a, st);
+    if constexpr (std::is_same<S, float>::value) {
+      if (a.nsweeps != 1) throw ArgError("general alpha: one sweep per launch");
+      launch_mg_t<56, 24, 4, false>(a, st);
+    } else {
+      throw ArgError("16-bit smoother: alpha = 1 only");
+    }
   } else if (a.nsweeps <= 3) {
     if (a.w >= 1200)
-      launch_mg_t<112, 50, 8, true, 512>(a, st);
+      launch_mg_t<112, 50, 8, true, 512, S>(a, st);
     else
-      launch_mg_t<48, 16, 8, true>(a, st);
+      launch_mg_t<48, 16, 8, true, 256, S>(a, st);
   } else if (a.nsweeps <= 5) {
-    launch_mg_t<40, 8, 12, true>(a, st);
+    launch_mg_t<40, 8, 12, true, 256, S>(a, st);
   } else {
     throw ArgError("smoother: at most 5 sweeps per launch");
   }
@@ -799,45 +937,69 @@ MgArgs level_args(MgLevel &L, const float *in, float *out, int ns, float alpha) 
   a.ihsq = 1.0f / L.hh / L.hh;
   a.nsweeps = ns;
   for (int k = 0; k < 5; k++) a.wsum[k] = (float)((double)(float)k + 0.0001);
+  a.rfac = 1.0f / 16.0f;
+  a.tile = -1;
   return a;
 }
 
-void run_tail(MgHier &mg, int lt, cudaStream_t st) {
+// Shared-memory bytes of the tail for levels lt .. levels-2 with arithmetic
+// type of elem_bytes.
+size_t tail_smem_bytes(const std::vector<MgLevel> &lv, int lt, size_t elem_bytes) {
+  size_t fw = 0, bw = 0;
+  for (int t = lt; t <= (int)lv.size() - 2; t++) {
+    size_t n = (size_t)lv[t].w * lv[t].h;
+    fw += 3 * ((n + 3) / 4 * 4);
+    bw += (n + 15) / 16 * 16;
+  }
+  return fw * elem_bytes + bw;
+}
+
+// scaled: the h^2-scaled form of the mixed solver (hh = 1, ihsq = 1,
+// restriction weights rfac[level]); else the reference's form.
+template <class S, class T>
+void run_tail_t(MgHier &mg, int lt, const S *rhs_top, S *e_top, const float *rfac,
+                cudaStream_t st) {
   ProfScope ps_(KC_TAIL, st);
-  TailArgs a{};
+  TailArgs<S> a{};
   int nl = mg.levels - 1 - lt;
   a.nlev = nl;
   size_t fw = 0, bw = 0;
   for (int t = 0; t < nl; t++) {
     MgLevel &L = mg.lv[lt + t];
-    TailLevel &T = a.L[t];
+    TailLevel &TL = a.L[t];
     int n = L.w * L.h;
-    T.w = L.w;
-    T.h = L.h;
-    T.hh = L.hh;
-    T.ihsq = 1.0f / L.hh / L.hh;
-    T.oe = (int)fw;
+    TL.w = L.w;
+    TL.h = L.h;
+    TL.hh = rfac ? 1.0f : L.hh;
+    TL.ihsq = rfac ? 1.0f : 1.0f / L.hh / L.hh;
+    TL.rfac = rfac ? rfac[lt + t] : 1.0f / 16.0f;
+    TL.oe = (int)fw;
     fw += (n + 3) / 4 * 4;
-    T.orr = (int)fw;
+    TL.orr = (int)fw;
     fw += (n + 3) / 4 * 4;
-    T.orhs = (int)fw;
+    TL.orhs = (int)fw;
     fw += (n + 3) / 4 * 4;
-    T.oc = (int)bw;
+    TL.oc = (int)bw;
     bw += (n + 15) / 16 * 16;
     a.code[t] = L.code;
     a.code_pitch[t] = L.pitch;
   }
   a.float_words = (int)fw;
   MgLevel &top = mg.lv[lt];
-  a.rhs_top = top.rhs;
+  a.rhs_top = rhs_top;
   a.rhs_pitch = top.pitch;
-  a.e_top = top.e[0];
+  a.e_top = e_top;
   a.e_pitch = top.pitch;
   for (int k = 0; k < 5; k++) a.wsum[k] = (float)((double)(float)k + 0.0001);
-  size_t smem = fw * 4 + bw;
-  k_mg_tail<<<1, dim3(32, 32), smem, st>>>(a);
+  size_t smem = fw * sizeof(T) + bw;
+  if (smem > TAIL_SMEM_MAX) throw ArgError("coarse levels exceed the tail kernel's shared memory");
+  k_mg_tail<S, T><<<1, dim3(32, 32), smem, st>>>(a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
+}
+
+void run_tail(MgHier &mg, int lt, cudaStream_t st) {
+  run_tail_t<float, float>(mg, lt, mg.lv[lt].rhs, mg.lv[lt].e[0], nullptr, st);
 }
 
 // MG::solveLevel, pressure_solver.cpp:201-248.
@@ -863,6 +1025,7 @@ void solve_level(MgHier &mg, std::vector<int> &cur, int l, bool zgbc, cudaStream
     MgArgs a = level_args(L, L.e[cur[l]], L.e[1 - cur[l]], 3, 1.0f);
     a.zgbc = bc;
     a.zero_init = l > 0;
+    a.tile = L.tile_pre;
     a.rc = C.rhs;
     a.cw = C.w;
     a.ch = C.h;
@@ -875,6 +1038,7 @@ void solve_level(MgHier &mg, std::vector<int> &cur, int l, bool zgbc, cudaStream
     ProfScope ps_(l == 0 ? KC_SMOOTH_L0 : (l == 1 ? KC_SMOOTH_L1 : KC_SMOOTH_COARSE), st);
     MgArgs a = level_args(L, L.e[cur[l]], L.e[1 - cur[l]], 3, 1.0f);
     a.zgbc = bc;
+    a.tile = L.tile_post;
     a.ec = C.e[cur[l + 1]];
     a.codec = C.code;
     a.cpitch = C.pitch;
@@ -886,17 +1050,297 @@ void solve_level(MgHier &mg, std::vector<int> &cur, int l, bool zgbc, cudaStream
   }
 }
 
+// ------------------------------------------------ mixed-precision solver
+// Defect correction (iterative refinement) around a 16-bit V-cycle.  The
+// outer loop keeps p, f and the residual in FP32 with FP64 norms; the inner
+// V-cycle solves the correction equation in the h^2-scaled form
+//   n e - sum(e_nbr) = g,  g = s h^2 r
+// (the smoother's own form with hh = 1: no 1/h^2 factors, so e and g share
+// one magnitude range), with s a power of two chosen from max|r| so that the
+// 16-bit values stay in range; the correction applied is e / s.
+template <class S>
+struct DcArgs {
+  const float *p;         // current pressure (FP32, level 0)
+  const S *e;             // correction of the last V-cycle (null: none yet)
+  const DcScalars *sc_in;  // its 1/s
+  float *pout;            // p + e / s with the zero-gradient edges
+  const float *f;
+  const uint8_t *code;
+  int w, h, pitch;
+  float ihsq;
+  float *r;          // residual of pout (0 on the edges)
+  DcScalars *sc;     // norm2 / maxbits accumulate here
+};
+
+// p' = p + e/s everywhere (edge cells take their interior neighbour's value,
+// corners untouched: setZeroGradientBC, pressure_solver.cpp:183-192), then
+// r = f + A p' (calculateResidualField, pressure_solver.cpp:100-110) with
+// ||r||^2 (FP32 per warp, FP64 across warps) and max|r|.
+template <class S>
+__global__ void __launch_bounds__(256) k_dc_resid(DcArgs<S> a) {
+  using St = Sto<S>;
+  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+  const int w = a.w, h = a.h;
+  const float is = a.e ? a.sc_in->inv_s : 0.0f;
+  auto PV = [&](int xx, int yy) {
+    if (yy >= 1 && yy <= h - 2) xx = xx == 0 ? 1 : (xx == w - 1 ? w - 2 : xx);
+    if (xx >= 1 && xx <= w - 2) yy = yy == 0 ? 1 : (yy == h - 1 ? h - 2 : yy);
+    size_t i = (size_t)yy * a.pitch + xx;
+    float v = __ldg(a.p + i);
+    if (a.e) v = v + St::ldg1(a.e + i) * is;
+    return v;
+  };
+  float rv = 0.0f;
+  if (x < w && y < h) {
+    size_t i = (size_t)y * a.pitch + x;
+    float pc = PV(x, y);
+    a.pout[i] = pc;
+    if (x >= 1 && x < w - 1 && y >= 1 && y < h - 1)
+      rv = resid1<float>(__ldg(a.code + i), pc, PV(x - 1, y), PV(x + 1, y), PV(x, y - 1),
+                         PV(x, y + 1), __ldg(a.f + i), a.ihsq);
+    a.r[i] = rv;
+  }
+  float sq = rv * rv;
+  unsigned mb = __float_as_uint(fabsf(rv));
+  for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+  mb = __reduce_max_sync(0xffffffffu, mb);
+  __shared__ double red[8];
+  __shared__ unsigned redm[8];
+  if (threadIdx.x == 0) {
+    red[threadIdx.y] = (double)sq;
+    redm[threadIdx.y] = mb;
+  }
+  __syncthreads();
+  if (threadIdx.y == 0 && threadIdx.x == 0) {
+    double t = 0.0;
+    unsigned m = 0;
+    for (int k = 0; k < 8; k++) {
+      t += red[k];
+      m = max(m, redm[k]);
+    }
+    atomicAdd(&a.sc->norm2, t);
+    atomicMax(&a.sc->maxbits, m);
+  }
+}
+
+// g = r * h0^2 * s into the 16-bit rhs of level 0, s = 2^-(ex + kexp) where
+// max|r| h0^2 = m 2^ex, m in [0.5, 1); records 1/s for the correction.
+template <class S>
+__global__ void __launch_bounds__(256) k_dc_scale(const float *__restrict__ r, S *g, int w, int h,
+                                                  int pitch, DcScalars *sc, float h0sq, int kexp) {
+  using St = Sto<S>;
+  const float m = __uint_as_float(sc->maxbits) * h0sq;
+  float mul = 0.0f, inv = 0.0f;
+  if (m > 0.0f) {
+    int ex;
+    frexpf(m, &ex);
+    mul = h0sq * ldexpf(1.0f, -ex - kexp);
+    inv = ldexpf(1.0f, ex + kexp);
+  }
+  const int x4 = (blockIdx.x * 32 + threadIdx.x) * 4, y = blockIdx.y * 8 + threadIdx.y;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) sc->inv_s = inv;
+  if (x4 >= w || y >= h) return;
+  const size_t i = (size_t)y * pitch + x4;
+  float4 v = __ldg(reinterpret_cast<const float4 *>(r + i));
+  v.x *= mul;
+  v.y *= mul;
+  v.z *= mul;
+  v.w *= mul;
+  St::st4(g + i, v);
+}
+
+// Mean of f over the interior fluid cells: sum, sum of squares and count
+// (FP32 within a warp, FP64 across warps), then f -= mean on those cells.
+// The zero-gradient system of the solver is singular (constants span its
+// null space); the tolerance and mixed solvers solve its compatible part.
+__global__ void __launch_bounds__(256) k_fmean_reduce(const float *__restrict__ f,
+                                                      const uint8_t *__restrict__ code, int w,
+                                                      int h, int pitch, double *acc) {
+  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+  float v = 0.0f;
+  bool in = false;
+  if (x >= 1 && x < w - 1 && y >= 1 && y < h - 1) {
+    size_t i = (size_t)y * pitch + x;
+    in = (__ldg(code + i) & C_CENTER) != 0;
+    if (in) v = __ldg(f + i);
+  }
+  float s1 = v, s2 = v * v;
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  int n = __popc(__ballot_sync(0xffffffffu, in));
+  __shared__ double r1[8], r2[8], rn[8];
+  if (threadIdx.x == 0) {
+    r1[threadIdx.y] = (double)s1;
+    r2[threadIdx.y] = (double)s2;
+    rn[threadIdx.y] = (double)n;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    double a1 = 0.0, a2 = 0.0, an = 0.0;
+    for (int k = 0; k < 8; k++) {
+      a1 += r1[k];
+      a2 += r2[k];
+      an += rn[k];
+    }
+    if (an > 0.0) {
+      atomicAdd(acc + 0, a1);
+      atomicAdd(acc + 1, a2);
+      atomicAdd(acc + 2, an);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_fmean_apply(float *f, const uint8_t *__restrict__ code,
+                                                     int w, int h, int pitch,
+                                                     const double *acc) {
+  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+  if (x < 1 || x >= w - 1 || y < 1 || y >= h - 1) return;
+  const double n = acc[2];
+  const float mean = n > 0.0 ? (float)(acc[0] / n) : 0.0f;
+  size_t i = (size_t)y * pitch + x;
+  if (__ldg(code + i) & C_CENTER) f[i] = f[i] - mean;
+}
+
+template <class S>
+MgArgsT<S> level_args_lo(MgHier &mg, MgLow &lo, int l, int cin, int ns) {
+  MgLevel &L = mg.lv[l];
+  MgArgsT<S> a{};
+  a.in = (const S *)lo.e[cin][l];
+  a.out = (S *)lo.e[1 - cin][l];
+  a.rhs = (const S *)lo.rhs[l];
+  a.code = L.code;
+  a.w = L.w;
+  a.h = L.h;
+  a.pitch = L.pitch;
+  a.hh = 1.0f;
+  a.alpha = 1.0f;
+  a.ihsq = 1.0f;
+  a.nsweeps = ns;
+  a.zero_init = 0;
+  for (int k = 0; k < 5; k++) a.wsum[k] = (float)((double)(float)k + 0.0001);
+  a.rfac = lo.rfac[l];
+  a.tile = -1;
+  return a;
+}
+
+// One V-cycle of the correction equation from e = 0 (solveLevel's schedule:
+// V(3,3), 5 sweeps on the coarsest level, zero-gradient edges on level 0).
+template <class S>
+void solve_level_lo(MgHier &mg, MgLow &lo, std::vector<int> &cur, int l, cudaStream_t st) {
+  const KernelClass kc = l == 0 ? KC_SMOOTH_L0 : (l == 1 ? KC_SMOOTH_L1 : KC_SMOOTH_COARSE);
+  if (l >= 1 && l == mg.tail_top) {
+    run_tail_t<S, double>(mg, l, (const S *)lo.rhs[l], (S *)lo.e[0][l], lo.rfac.data(), st);
+    cur[l] = 0;
+    return;
+  }
+  if (l == mg.levels - 2) {
+    ProfScope ps_(kc, st);
+    MgArgsT<S> a = level_args_lo<S>(mg, lo, l, cur[l], 5);
+    a.zero_init = 1;
+    a.zgbc = l == 0;
+    launch_mg(a, st);
+    cur[l] ^= 1;
+    return;
+  }
+  MgLevel &C = mg.lv[l + 1];
+  {
+    ProfScope ps_(kc, st);
+    MgArgsT<S> a = level_args_lo<S>(mg, lo, l, cur[l], 3);
+    a.zero_init = 1;
+    a.zgbc = l == 0;
+    a.tile = mg.lv[l].tile_pre;
+    a.rc = (S *)lo.rhs[l + 1];
+    a.cw = C.w;
+    a.ch = C.h;
+    a.cpitch = C.pitch;
+    launch_mg(a, st);
+    cur[l] ^= 1;
+  }
+  solve_level_lo<S>(mg, lo, cur, l + 1, st);
+  {
+    ProfScope ps_(kc, st);
+    MgArgsT<S> a = level_args_lo<S>(mg, lo, l, cur[l], 3);
+    a.zgbc = l == 0;
+    a.tile = mg.lv[l].tile_post;
+    a.ec = (const S *)lo.e[cur[l + 1]][l + 1];
+    a.codec = C.code;
+    a.cpitch = C.pitch;
+    a.cw = C.w;
+    a.ch = C.h;
+    launch_mg(a, st);
+    cur[l] ^= 1;
+  }
+}
+
+// One residual pass: p <- p + e/s (e = null: none), r, norm, max.
+template <class S>
+void dc_resid(MgHier &mg, MgLow &lo, const S *e, cudaStream_t st) {
+  ProfScope ps_(KC_RESIDUAL, st);
+  MgLevel &L = mg.lv[0];
+  UBG_CUDA(cudaMemsetAsync(lo.dev, 0, offsetof(DcScalars, inv_s), st));
+  DcArgs<S> a{};
+  a.p = L.e[mg.cur0];
+  a.e = e;
+  a.sc_in = lo.dev;
+  a.pout = L.e[1 - mg.cur0];
+  a.f = L.rhs;
+  a.code = L.code;
+  a.w = L.w;
+  a.h = L.h;
+  a.pitch = L.pitch;
+  a.ihsq = 1.0f / L.hh / L.hh;
+  a.r = lo.r32;
+  a.sc = lo.dev;
+  dim3 grid((L.w + 31) / 32, (L.h + 7) / 8);
+  k_dc_resid<S><<<grid, dim3(32, 8), 0, st>>>(a);
+  UBG_LAUNCH_CHECK();
+  g_stats.launches++;
+  mg.cur0 ^= 1;
+}
+
+template <class S>
+int solve_mixed_t(MgHier &mg, MgLow &lo, double tol, int max_cycles, double fnorm2, double *rel,
+                  cudaStream_t st) {
+  MgLevel &L0 = mg.lv[0];
+  const float h0sq = L0.hh * L0.hh;
+  const S *e_last = nullptr;
+  int c = 0;
+  auto converged = [&]() {
+    UBG_CUDA(cudaMemcpyAsync(lo.host, lo.dev, sizeof(DcScalars), cudaMemcpyDeviceToHost, st));
+    UBG_CUDA(cudaStreamSynchronize(st));
+    return lo.host->norm2 <= tol * tol * fnorm2;
+  };
+  for (;;) {
+    dc_resid<S>(mg, lo, e_last, st);
+    if (tol > 0.0 && converged()) break;
+    if (c >= max_cycles) break;
+    {
+      ProfScope ps_(KC_RESIDUAL, st);
+      dim3 grid((L0.w + 127) / 128, (L0.h + 7) / 8);
+      k_dc_scale<S><<<grid, dim3(32, 8), 0, st>>>(lo.r32, (S *)lo.rhs[0], L0.w, L0.h, L0.pitch,
+                                                  lo.dev, h0sq, lo.kexp);
+      UBG_LAUNCH_CHECK();
+      g_stats.launches++;
+    }
+    std::vector<int> cur(mg.levels, 0);
+    solve_level_lo<S>(mg, lo, cur, 0, st);
+    e_last = (const S *)lo.e[cur[0]][0];
+    c++;
+  }
+  if (rel) *rel = tol > 0.0 ? std::sqrt(lo.host->norm2 / (fnorm2 > 0.0 ? fnorm2 : 1.0)) : -1.0;
+  return c;
+}
+
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
-int choose_tail(const std::vector<MgLevel> &lv) {
+int choose_tail(const std::vector<MgLevel> &lv, int max_cells) {
   int L = (int)lv.size();
   for (int lt = 1; lt <= L - 2; lt++) {
-    size_t bytes = 0;
-    for (int t = lt; t <= L - 2; t++) {
-      size_t n = (size_t)lv[t].w * lv[t].h;
-      bytes += 3 * ((n + 3) / 4 * 4) * 4 + (n + 15) / 16 * 16;
-    }
-    if (bytes <= TAIL_SMEM_MAX && (size_t)lv[lt].w * lv[lt].h <= 2048) return lt;
+    // sized for the FP64 arithmetic of the mixed solver's coarse solve
+    if (tail_smem_bytes(lv, lt, 8) <= TAIL_SMEM_MAX && (size_t)lv[lt].w * lv[lt].h <= (size_t)max_cells)
+      return lt;
   }
   return -1;
 }
@@ -955,7 +1399,7 @@ void mg_bind(MgHier &mg, int W, int H, float h0, void *arena, size_t bytes) {
   }
   mg.norm = (double *)p;
   mg.post_norm2 = nullptr;
-  mg.tail_top = choose_tail(lv);
+  mg.tail_top = choose_tail(lv, mg.tail_cells);
   mg.lv = lv;
   mg.levels = (int)lv.size();
   mg.arena = nullptr;  // not owned
@@ -1015,6 +1459,207 @@ void mg_solve(MgHier &mg, bool zgbc, cudaStream_t st) {
   cur[0] = mg.cur0;
   solve_level(mg, cur, 0, zgbc, st);
   mg.cur0 = cur[0];
+}
+
+double mg_meanfree_rhs(MgHier &mg, cudaStream_t st, bool want_norm) {
+  ProfScope ps_(KC_RESIDUAL, st);
+  MgLevel &L = mg.lv[0];
+  double *acc = mg.norm + 8;
+  UBG_CUDA(cudaMemsetAsync(acc, 0, 3 * sizeof(double), st));
+  dim3 grid((L.w + 31) / 32, (L.h + 7) / 8);
+  k_fmean_reduce<<<grid, dim3(32, 8), 0, st>>>(L.rhs, L.code, L.w, L.h, L.pitch, acc);
+  UBG_LAUNCH_CHECK();
+  k_fmean_apply<<<grid, dim3(32, 8), 0, st>>>(L.rhs, L.code, L.w, L.h, L.pitch, acc);
+  UBG_LAUNCH_CHECK();
+  g_stats.launches += 2;
+  if (!want_norm) return -1.0;
+  double h[3];
+  UBG_CUDA(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, st));
+  UBG_CUDA(cudaStreamSynchronize(st));
+  return h[2] > 0.0 ? std::max(0.0, h[1] - h[0] * h[0] / h[2]) : h[1];
+}
+
+// ------------------------------------------------------------- autotuner
+namespace {
+struct EvPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  EvPair() {
+    UBG_CUDA(cudaEventCreate(&a));
+    UBG_CUDA(cudaEventCreate(&b));
+  }
+  ~EvPair() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+// Mean milliseconds of `reps` calls of f after `warm` untimed calls.
+template <class F>
+double time_ms(EvPair &ev, cudaStream_t st, int warm, int reps, F &&f) {
+  for (int i = 0; i < warm; i++) f();
+  UBG_CUDA(cudaEventRecord(ev.a, st));
+  for (int i = 0; i < reps; i++) f();
+  UBG_CUDA(cudaEventRecord(ev.b, st));
+  UBG_CUDA(cudaEventSynchronize(ev.b));
+  float ms = 0.0f;
+  UBG_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+  return (double)ms / reps;
+}
+}  // namespace
+
+void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
+  init_kernel_attributes();
+  const int nl = mg.levels;
+  EvPair ev;
+  const int warm = 2, reps = 5;
+  // the tail sizes to try, and the deepest level any of them leaves tiled
+  const int tail_cand[] = {512, 1024, 2048, 4096};
+  int deepest = nl - 2;
+  for (int tc : tail_cand) {
+    int lt = choose_tail(mg.lv, tc);
+    if (lt >= 1) deepest = std::max(1, std::min(deepest, std::max(lt, 1)));
+  }
+  std::vector<double> best_pre(nl, 0.0), best_post(nl, 0.0);
+  std::string rep = "{\"levels\": [";
+  // per level (not the coarsest): the pre-smoothing launch (3 sweeps +
+  // residual + restriction) and the post-smoothing launch (prolongation +
+  // correction + 3 sweeps) with each candidate tile.  Trials read the
+  // level's current arrays and write only its idle ping-pong buffer and the
+  // next level's rhs: the solver state is unchanged.
+  int last_tiled = std::max(0, std::min(nl - 3, std::max(deepest, mg.tail_top >= 1 ? mg.tail_top : nl - 2) - 1));
+  for (int l = 0; l <= last_tiled; l++) {
+    MgLevel &L = mg.lv[l], &C = mg.lv[l + 1];
+    int cur = l == 0 ? mg.cur0 : 0;
+    double tpre[kTiles], tpost[kTiles];
+    int bp = -1, bq = -1;
+    for (int id = 0; id < kTiles; id++) {
+      MgArgs a = level_args(L, L.e[cur], L.e[1 - cur], 3, 1.0f);
+      a.zgbc = l == 0;
+      a.zero_init = l > 0;
+      a.rc = C.rhs;
+      a.cw = C.w;
+      a.ch = C.h;
+      a.cpitch = C.pitch;
+      tpre[id] = time_ms(ev, st, warm, reps, [&] { launch_mg_tile(a, id, st); });
+      MgArgs b = level_args(L, L.e[cur], L.e[1 - cur], 3, 1.0f);
+      b.zgbc = l == 0;
+      b.ec = C.e[0];
+      b.codec = C.code;
+      b.cpitch = C.pitch;
+      b.cw = C.w;
+      b.ch = C.h;
+      tpost[id] = time_ms(ev, st, warm, reps, [&] { launch_mg_tile(b, id, st); });
+      if (bp < 0 || tpre[id] < tpre[bp]) bp = id;
+      if (bq < 0 || tpost[id] < tpost[bq]) bq = id;
+    }
+    L.tile_pre = bp;
+    L.tile_post = bq;
+    best_pre[l] = tpre[bp];
+    best_post[l] = tpost[bq];
+    char buf[320];
+    snprintf(buf, sizeof(buf),
+             "%s{\"level\": %d, \"w\": %d, \"h\": %d, \"pre\": \"%s\", \"pre_us\": %.2f, "
+             "\"post\": \"%s\", \"post_us\": %.2f}",
+             l ? ", " : "", l, L.w, L.h, kTileNames[bp], 1e3 * tpre[bp], kTileNames[bq],
+             1e3 * tpost[bq]);
+    rep += buf;
+  }
+  rep += "], \"tail\": [";
+  // the tail size: tail time + the tiled launches of the levels above it
+  int best_tc = mg.tail_cells, best_lt = mg.tail_top;
+  double best_cost = -1.0;
+  bool first = true;
+  for (int tc : tail_cand) {
+    int lt = choose_tail(mg.lv, tc);
+    if (lt < 1 || lt - 1 > last_tiled) continue;
+    double t = time_ms(ev, st, warm, reps, [&] { run_tail(mg, lt, st); });
+    double cost = t;
+    for (int l = 0; l < lt; l++) cost += best_pre[l] + best_post[l];
+    char buf[160];
+    snprintf(buf, sizeof(buf), "%s{\"cells\": %d, \"top\": %d, \"tail_us\": %.2f, \"vcycle_us\": %.2f}",
+             first ? "" : ", ", tc, lt, 1e3 * t, 1e3 * cost);
+    rep += buf;
+    first = false;
+    if (best_cost < 0.0 || cost < best_cost) {
+      best_cost = cost;
+      best_tc = tc;
+      best_lt = lt;
+    }
+  }
+  mg.tail_cells = best_tc;
+  mg.tail_top = best_lt;
+  char buf[96];
+  snprintf(buf, sizeof(buf), "], \"tail_cells\": %d, \"tail_top\": %d}", best_tc, best_lt);
+  rep += buf;
+  if (report) *report += rep;
+}
+
+void mg_low_alloc(MgLow &lo, const MgHier &mg, int prec) {
+  mg_low_free(lo);
+  if (prec != UBG_MIXED_FP16 && prec != UBG_MIXED_BF16) throw ArgError("unknown precision mode");
+  init_kernel_attributes();
+  size_t total = align256(sizeof(DcScalars));
+  for (auto &L : mg.lv) total += 3 * align256((size_t)L.pitch * L.h * 2);
+  const MgLevel &L0 = mg.lv[0];
+  total += align256((size_t)L0.pitch * L0.h * 4);
+  void *arena = nullptr;
+  if (cudaMalloc(&arena, total) != cudaSuccess) {
+    cudaGetLastError();
+    throw std::bad_alloc();
+  }
+  UBG_CUDA(cudaMemset(arena, 0, total));
+  void *host = nullptr;
+  if (cudaHostAlloc(&host, sizeof(DcScalars), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(arena);
+    throw std::bad_alloc();
+  }
+  char *p = (char *)arena;
+  lo.dev = (DcScalars *)p;
+  p += align256(sizeof(DcScalars));
+  lo.r32 = (float *)p;
+  p += align256((size_t)L0.pitch * L0.h * 4);
+  for (int k = 0; k < 2; k++) lo.e[k].assign(mg.levels, nullptr);
+  lo.rhs.assign(mg.levels, nullptr);
+  lo.rfac.assign(mg.levels, 0.0f);
+  for (int l = 0; l < mg.levels; l++) {
+    size_t b = align256((size_t)mg.lv[l].pitch * mg.lv[l].h * 2);
+    lo.e[0][l] = p;
+    p += b;
+    lo.e[1][l] = p;
+    p += b;
+    lo.rhs[l] = p;
+    p += b;
+    if (l + 1 < mg.levels) {
+      double q = (double)mg.lv[l + 1].hh / (double)mg.lv[l].hh;
+      lo.rfac[l] = (float)(q * q / 16.0);
+    }
+  }
+  // e = A^-1 g is bounded by about max|g| * max(W, H)^2 / 2 (a channel with
+  // one Dirichlet end); keep it below 2^14 in FP16.  BF16 has FP32's range.
+  int kexp = 0;
+  if (prec == UBG_MIXED_FP16) {
+    double n = (double)std::max(L0.w, L0.h);
+    kexp = std::max(0, (int)std::ceil(std::log2(0.5 * n * n)) - 14);
+  }
+  lo.kexp = kexp;
+  lo.prec = prec;
+  lo.levels = mg.levels;
+  lo.arena = arena;
+  lo.host = (DcScalars *)host;
+}
+
+void mg_low_free(MgLow &lo) {
+  if (lo.arena) cudaFree(lo.arena);
+  if (lo.host) cudaFreeHost(lo.host);
+  lo = MgLow{};
+}
+
+int mg_solve_mixed(MgHier &mg, MgLow &lo, double tol, int max_cycles, double fnorm2, double *rel,
+                   cudaStream_t st) {
+  if (lo.levels != mg.levels) throw std::runtime_error("mixed-precision hierarchy not allocated");
+  if (lo.prec == UBG_MIXED_FP16) return solve_mixed_t<__half>(mg, lo, tol, max_cycles, fnorm2, rel, st);
+  return solve_mixed_t<__nv_bfloat16>(mg, lo, tol, max_cycles, fnorm2, rel, st);
 }
 
 void mg_set_h(MgHier &mg, float h0) {

@@ -119,6 +119,17 @@ void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const Ste
 void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, float pwidth,
                 unsigned int *umax_bits, StepScalars *sc, cudaStream_t st, bool umax_ready);
 
+// ------------------------------------------------- game-side field access
+void launch_scatter_accum(float *ax, float *ay, int P, int W, int H, const float2 *xy,
+                          const float2 *v, int n, cudaStream_t st);
+void launch_sample_velocity(const float *vx, const float *vy, int P, int W, int H,
+                            const float2 *xy, float2 *out, int n, cudaStream_t st);
+void launch_set_grids(const int2 *cells, const uint8_t *val, const uint8_t *zero, int n,
+                      uint8_t *flag, float *vx, float *vy, float *p, int P, int W, int H,
+                      cudaStream_t st);
+void launch_shift_map(VelBufs &v, int fx, int fy, const float *p_in, float *p_out,
+                      const uint8_t *flag, int P, int W, int H, float inlet_u, cudaStream_t st);
+
 // ------------------------------------------------------------ multigrid
 struct MgLevel {
   int w, h, pitch;
@@ -127,6 +138,8 @@ struct MgLevel {
   uint8_t *code;       // per-cell stencil code (own flag + the 4 neighbours' flags)
   float *e[2];         // level 0: pressure ping-pong; coarse: error ping-pong
   float *rhs;          // level 0: f; coarse: restricted residual
+  int tile_pre = -1;   // smoother tile of the pre- / post-smoothing launch
+  int tile_post = -1;  //   (-1: chosen by level width; else set by the autotuner)
 };
 
 struct MgHier {
@@ -134,11 +147,18 @@ struct MgHier {
   std::vector<MgLevel> lv;
   int cur0 = 0;                  // which e[] of level 0 holds p
   int tail_top = -1;             // first level solved by the one-CTA tail kernel
+  int tail_cells = 2048;         // largest top level the tail takes (autotuned)
   void *arena = nullptr;
   size_t arena_bytes = 0;
   double *norm = nullptr;        // device scalar for residual norms
   double *post_norm2 = nullptr;  // if set: ||r||^2 after each level-0 post-smoothing
 };
+
+// Times the candidate smoother tiles of every level and the tail sizes on
+// this hierarchy's own arrays (state preserved: trials write only scratch
+// buffers) and keeps the fastest; results are bit-identical for every
+// choice.  Appends a JSON report to *report if given.
+void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report);
 
 // Allocates the hierarchy for a W x H level-0 grid with spacing h0.
 void mg_alloc(MgHier &mg, int W, int H, float h0);
@@ -164,6 +184,45 @@ void level_rbgs(MgLevel &L, int &cur, float alpha, cudaStream_t st);
 // Residual field of one level into `r` (pitched like the level, may be null)
 // with its squared L2 norm accumulated into *norm2 (device double, may be null).
 void level_residual(const MgLevel &L, int cur, float *r, double *norm2, cudaStream_t st);
+
+// ------------------------------------------- mixed-precision multigrid
+// Device scalars of the defect-correction loop.
+struct DcScalars {
+  double norm2;      // ||r||^2 of the last residual pass (FP64)
+  unsigned maxbits;  // max |r| of the last residual pass, as float bits
+  float inv_s;       // 1 / s of the correction in flight (s = scale of the 16-bit rhs)
+};
+
+// Low-precision correction hierarchy: the level shapes and stencil codes of
+// an MgHier, error and right-hand side stored in 16 bits (FP16 or BF16).
+struct MgLow {
+  int prec = 0;  // UBG_MIXED_FP16 or UBG_MIXED_BF16
+  int levels = 0;
+  std::vector<void *> e[2], rhs;  // per level, pitch of the MgHier level
+  std::vector<float> rfac;        // restriction weight of each fine level, scaled form
+  float *r32 = nullptr;           // level-0 residual in FP32
+  DcScalars *dev = nullptr;       // device scalars
+  DcScalars *host = nullptr;      // pinned copy for the convergence test
+  void *arena = nullptr;
+  int kexp = 0;  // the scaled rhs g satisfies max|g| in [2^-(kexp+1), 2^-kexp)
+};
+
+// Subtracts the mean of level 0's rhs over the interior fluid cells from
+// those cells (device-side; capturable).  With want_norm, synchronises and
+// returns ||f - mean||^2 over them (FP64), else -1.
+double mg_meanfree_rhs(MgHier &mg, cudaStream_t st, bool want_norm);
+void mg_low_alloc(MgLow &lo, const MgHier &mg, int prec);
+void mg_low_free(MgLow &lo);
+
+// Mixed-precision MG::solve of level 0 of `mg` (p = e[cur0], rhs f): an FP32
+// defect-correction loop whose correction is one V-cycle of the scaled
+// system in 16-bit storage (FP32 arithmetic, FP64 coarse solve).  Runs
+// max_cycles corrections; when tol > 0 it stops as soon as
+// ||r|| <= tol * sqrt(fnorm2) (FP64 norms, one host read per cycle).
+// Returns the corrections run; *rel (may be null) = ||r|| / sqrt(fnorm2) of
+// the final p when tol > 0, else -1.
+int mg_solve_mixed(MgHier &mg, MgLow &lo, double tol, int max_cycles, double fnorm2, double *rel,
+                   cudaStream_t st);
 
 // ------------------------------------------------------------- tracers
 struct TracerArgs {

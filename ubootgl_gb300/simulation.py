@@ -62,12 +62,17 @@ class Simulation:
 
     # ------------------------------------------------------------ options
     def set_options(self, solver_mode=None, vcycles=None, tol=None, max_vcycles=None,
-                    use_graph=None):
+                    use_graph=None, precision=None):
+        """Solver options (extension).  precision: "fp32", "fp16" or "bf16"
+        (the mixed-precision defect-correction solver)."""
         o = L.Options()
         L.check(self._lib.ubg_default_options(C.byref(o)))
         cur = getattr(self, "_opts", None)
         if cur is not None:
-            o = cur
+            C.memmove(C.byref(o), C.byref(cur), C.sizeof(o))
+        if precision is not None:
+            o.precision = {"fp32": L.FP32, "fp16": L.MIXED_FP16,
+                           "bf16": L.MIXED_BF16}.get(precision, precision)
         if solver_mode is not None:
             o.solver_mode = solver_mode
         if vcycles is not None:
@@ -99,6 +104,13 @@ class Simulation:
         v = C.c_float()
         L.check(self._lib.ubg_last_dt(self._h, C.byref(v)))
         return v.value
+
+    def solver_stats(self):
+        """(V-cycles or corrections of the last solve, final ||r||/||f|| in
+        tolerance mode else -1)."""
+        n, r = C.c_int(), C.c_double()
+        L.check(self._lib.ubg_solver_stats(self._h, C.byref(n), C.byref(r)))
+        return n.value, r.value
 
     def applyAccumulatedVelocity(self):
         L.check(self._lib.ubg_apply_accumulated_velocity(self._h))
