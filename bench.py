@@ -252,6 +252,19 @@ def run_ours(args):
             modes["mixed_" + prec] = time_mode(L, lib, flag, vx, vy, prec, args.mode_steps,
                                                args.warmup, dev)
 
+    # ---- batched uneven instances and the served stream (extensions)
+    batched, served = {}, {}
+    if args.batch > 0:
+        for prec in args.batch_precisions.split(","):
+            batched[prec] = batch_bench(L, lib, args.batch, args.batch_steps, args.warmup, prec)
+    if args.serve_sessions > 0:
+        for prec in args.serve_precisions.split(","):
+            for rate, dur in ((args.serve_rate, args.serve_seconds),
+                              (args.serve_rate_low, args.serve_seconds)):
+                served["%s_%g_per_s" % (prec, rate)] = serve_bench(
+                    L, lib, args.serve_sessions, rate, dur, args.serve_budget_gb,
+                    args.serve_active, prec)
+
     if rank != 0:
         return
     line = {
@@ -271,6 +284,8 @@ def run_ours(args):
         "kernels": kt["detail"],
         "profiled_step_ms": kt["profiled_step_ms"],
         "modes": modes,
+        "batched": batched,
+        "served": served,
     }
     if not args.no_cpu_baseline:
         val, info = time_cpu_step(W, H, budget_s=args.cpu_budget)
@@ -314,6 +329,128 @@ def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev):
                       "solve" % precision, "fields_finite": finite}
 
 
+def batch_bench(L, lib, n, steps, warmup, precision, seed=11):
+    """Batched uneven instances: n simulations, widths log-uniform in
+    [128, 2048] (multiples of 32), height = width / 2, each with its own
+    seeded disc mask (8-15 % solid) and inflow speed (uniform [0.5, 1.5]);
+    every member autotuned; all advance one step per batch graph launch.
+    Host wall clock around K batch steps (synchronised), against the same
+    members stepped one call each on their own streams."""
+    from ubootgl_gb300 import workload as WL
+    from ubootgl_gb300.simulation import Batch, Simulation
+    widths = WL.log_uniform_widths(n, 128, 2048, seed)
+    sims, cells = [], 0
+    for i, W in enumerate(widths):
+        H = W // 2
+        flag, vx, vy = WL.instance(W, H, seed * 1000 + i)
+        sim = Simulation(flag, 1.0, 1e-4)
+        if precision != "fp32":
+            sim.set_options(precision=precision)
+        for nm, a in (("vx", vx), ("vy", vy), ("vx_back", vx), ("vy_back", vy)):
+            sim.set(nm, a)
+        sims.append(sim)
+        cells += W * H
+    t0 = time.perf_counter()
+    for sim in sims:
+        sim.autotune()
+    t_tune = time.perf_counter() - t0
+    batch = Batch(sims)
+    for _ in range(max(3, warmup)):
+        batch.step(cfl=0.5)
+    batch.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        batch.step(cfl=0.5)
+    batch.sync()
+    for s in sims:
+        s.sync()
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for s in sims:
+            s.step_cfl(0.5)
+    for s in sims:
+        s.sync()
+    t_seq = time.perf_counter() - t0
+    finite = all(bool(np.isfinite(s.get("p")).all()) for s in sims[:4])
+    batch.close()
+    for s in sims:
+        s.close()
+    return {"value": round(cells * steps / t_batch / 1e6, 2), "unit": "Mcell-steps/s",
+            "instances": n, "total_cells": cells, "steps": steps,
+            "ms_per_batch_step": round(1e3 * t_batch / steps, 4),
+            "one_call_per_member_value": round(cells * steps / t_seq / 1e6, 2),
+            "autotune_s": round(t_tune, 2), "precision": precision, "fields_finite": finite,
+            "widths": "log-uniform [128, 2048], h = w/2", "timing": "host wall clock, synchronised"}
+
+
+def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, precision, seed=5):
+    """Served stream: step requests arrive as a Poisson process (`rate` per
+    second for `duration` seconds) over n_sessions resident sessions with
+    widths log-uniform in [256, 4096] (height = width / 2), each asking for
+    k ~ U[1, 20] device-CFL steps; sessions admitted under a device-memory
+    budget.  Session fields are crops of one seeded 4096 x 2048 instance
+    (walls re-applied, own inflow speed)."""
+    from ubootgl_gb300 import workload as WL
+    from ubootgl_gb300.simulation import Server
+    rng = np.random.default_rng(seed)
+    base_flag, base_vx, base_vy = WL.instance(4096, 2048, seed)
+    srv = Server(int(budget_gb * (1 << 30)), max_active=max_active)
+    ids, cells = [], {}
+    for W in WL.log_uniform_widths(n_sessions, 256, 4096, seed + 1):
+        H = W // 2
+        flag = base_flag[:H, :W].copy()
+        flag[0, :] = 0.0
+        flag[H - 1, :] = 0.0
+        u = np.float32(rng.uniform(0.5, 1.5))
+        vx = base_vx[:H, :W - 1].copy()
+        vy = base_vy[:H - 1, :W].copy()
+        vx[:, 0] = u
+        vx *= flag[:, :-1] * flag[:, 1:]
+        vy *= flag[:-1, :] * flag[1:, :]
+        vy[0, :] = 0.0
+        sid = srv.open(flag, vx, vy, precision=precision)
+        if sid is not None:
+            ids.append(sid)
+            cells[sid] = W * H
+    rejected = srv.stats()["rejected_sessions"]
+    # warm every session once (graph capture, first-touch), outside the stream
+    for r in [srv.submit(s, 1) for s in ids]:
+        srv.wait(r)
+    srv2_base = srv.stats()
+    t = 0.0
+    arrivals = []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        arrivals.append((t, ids[int(rng.integers(len(ids)))], int(rng.integers(1, 21))))
+    offered = sum(cells[s] * k for _, s, k in arrivals) / duration
+    t0 = time.perf_counter()
+    reqs = []
+    for at, s, k in arrivals:
+        d = at - (time.perf_counter() - t0)
+        if d > 0:
+            time.sleep(d)
+        reqs.append(srv.submit(s, k))
+    srv.drain()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    lat = np.array([srv.wait(r) for r in reqs]) if reqs else np.zeros(1)
+    srv.close()
+    done = st["completed"] - srv2_base["completed"]
+    cs = st["cell_steps"] - srv2_base["cell_steps"]
+    return {"sessions": len(ids), "rejected_sessions": rejected, "requests": len(arrivals),
+            "completed": done, "rate_per_s": rate, "duration_s": duration,
+            "p50_ms": round(float(np.percentile(lat, 50)), 3),
+            "p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "max_ms": round(float(lat.max()), 3),
+            "value": round(cs / wall / 1e6, 2), "unit": "Mcell-steps/s",
+            "offered_mcell_steps_per_s": round(offered / 1e6, 1),
+            "device_gb": round(st["device_bytes_used"] / 2 ** 30, 2), "budget_gb": budget_gb,
+            "max_active": max_active, "precision": precision, "wall_s": round(wall, 2)}
+
+
 def working_set_bytes(W, H):
     n = W * H
     return n * (4 * 4 + 4 * 2 + 4 * 2 + 1) * 4 // 3 + n * 4 * 2
@@ -331,6 +468,19 @@ ALG_BYTES_PER_CELL = {
     "divergence": 8 + 4,
     "gradient": 4 + 1 + 8 + 8,
 }
+
+
+def profiled_traffic(W, H):
+    """DRAM bytes (read + write) per level-0 k_mg launch from the committed
+    ncu summary of this workload, or None if there is none for this size."""
+    fn = os.path.join(ROOT, "profiles", "k_mg_level0_%dx%d.txt" % (W, H))
+    try:
+        for line in open(fn):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
 
 
 def kernel_timing(sim, lib, W, H, reps=30):
@@ -366,11 +516,11 @@ def kernel_timing(sim, lib, W, H, reps=30):
     compulsory = 13.0 * cells
     achieved = alg / (ms_l / 1e3) / 1e9
     ach_c = compulsory / (ms_l / 1e3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_smooth level 0 (3 red-black sweeps per launch, "
+    roof = {"bound": "hbm", "kernel": "k_mg level 0 (3 red-black sweeps per launch, "
                                       "temporally blocked in shared memory)",
             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 3), "peak_source": peak_src,
-            "traffic": None, "launch_ms": round(ms_l, 5),
+            "traffic": profiled_traffic(W, H), "launch_ms": round(ms_l, 5),
             "alg_bytes_per_launch": alg,
             "achieved_compulsory": round(ach_c, 1),
             "frac_compulsory": round(ach_c / peak, 3),
@@ -442,6 +592,16 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--mode-steps", type=int, default=500,
                     help="timed steps per mixed-precision mode (0: skip)")
+    ap.add_argument("--batch", type=int, default=64, help="batched instances (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--batch-precisions", default="fp32,fp16")
+    ap.add_argument("--serve-sessions", type=int, default=128, help="served sessions (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-rate-low", type=float, default=100.0)
+    ap.add_argument("--serve-seconds", type=float, default=1.5)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-active", type=int, default=32)
+    ap.add_argument("--serve-precisions", default="fp32")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -207,6 +207,72 @@ int ubg_snapshot_bytes(ubg_sim *sim, size_t *bytes);
 int ubg_snapshot(ubg_sim *sim, void *dst);
 int ubg_restore(ubg_sim *sim, const void *src);
 
+/* ------------------------------------------- autotuner and batches */
+
+/* Autotuner (extension): times the candidate smoother tiles of every
+ * multigrid level (pre- and post-smoothing launches separately) and the
+ * sizes of the one-CTA coarse tail on this simulation's own arrays, and
+ * keeps the fastest.  The simulation's state is unchanged and results are
+ * bit-identical for every choice.  report (may be NULL) receives a JSON
+ * object with the per-level choices and times (truncated to len). */
+int ubg_autotune(ubg_sim *sim, char *report, size_t len);
+
+/* Batch (extension): n independent simulations of any sizes advanced
+ * together.  Each batch step is one CUDA graph launch whose parallel
+ * branches are the members' fixed-cycle step bodies, so their kernels run
+ * concurrently.  dts: n host time steps, or NULL for dt = cfl * h / max|u|
+ * per member on the device.  Members keep their own fields, options and
+ * streams (ordered after the batch step); each member's result is
+ * bit-identical to stepping it alone.  Members need UBG_SOLVE_FIXED and no
+ * pending sinks.  The batch does not own the members. */
+typedef struct ubg_batch ubg_batch;
+int ubg_batch_create(int n, ubg_sim *const *sims, ubg_batch **out);
+int ubg_batch_destroy(ubg_batch *batch);
+int ubg_batch_step(ubg_batch *batch, const float *dts, float cfl);
+int ubg_batch_stream(ubg_batch *batch, void **stream);
+int ubg_batch_sync(ubg_batch *batch);
+
+/* Device bytes a simulation of width x height holds (fields + multigrid,
+ * FP32 solver), and the bytes a live handle holds now. */
+int ubg_device_bytes(int width, int height, size_t *bytes);
+int ubg_sim_device_bytes(ubg_sim *sim, size_t *bytes);
+
+/* ------------------------------------------------------------ step server */
+
+/* Step server (extension): continuous batching of step requests over
+ * sessions whose fields stay resident on the device.  Sessions are admitted
+ * against a device-memory budget when opened (UBG_EBUSY and a rejection
+ * count when the budget is exhausted).  A request asks for `steps` device-CFL
+ * steps of one session.  A worker thread admits queued requests in arrival
+ * order while fewer than max_active are in flight (one per session),
+ * enqueues each admitted request's steps on its session's stream and
+ * retires requests as their streams complete, so requests arriving while
+ * others run join as slots free up and the device overlaps all in-flight
+ * sessions.  Latency = completion - submission. */
+typedef struct ubg_server ubg_server;
+typedef struct ubg_serve_stats {
+  int sessions, queued, active;
+  long long completed, rejected_sessions, cell_steps;
+  size_t device_bytes_used;
+  double busy_ms;              /* first admission to last completion */
+  double p50_ms, p99_ms, max_ms; /* request latencies so far */
+} ubg_serve_stats;
+int ubg_server_create(size_t budget_bytes, int max_active, ubg_server **out);
+int ubg_server_destroy(ubg_server *srv);
+/* Opens a session (Simulation(flag, pwidth, mu); vx / vy may be NULL, else
+ * they initialise both buffers; opt may be NULL). */
+int ubg_server_open(ubg_server *srv, const float *flag, int width, int height, float pwidth,
+                    float mu, const float *vx, const float *vy, const ubg_options *opt,
+                    int *session);
+int ubg_server_close(ubg_server *srv, int session);
+int ubg_server_submit(ubg_server *srv, int session, int steps, float cfl, uint64_t *request);
+int ubg_server_wait(ubg_server *srv, uint64_t request, double *latency_ms);
+int ubg_server_drain(ubg_server *srv);
+/* The session's simulation handle, for reading its fields while it has no
+ * request in flight. */
+int ubg_server_session_sim(ubg_server *srv, int session, ubg_sim **sim);
+int ubg_server_stats(ubg_server *srv, ubg_serve_stats *out);
+
 /* Multigrid of the simulation: number of levels, size and (float) flag of
  * one level (MG::flagcs, pressure_solver.hpp:72). */
 int ubg_mg_levels(ubg_sim *sim, int *levels);

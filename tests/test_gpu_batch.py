@@ -1,0 +1,108 @@
+"""Batches and the autotuner: results identical to stepping alone.
+
+A batch step captures every member's fixed-cycle step body as a parallel
+branch of one CUDA graph; the members only touch their own memory and the
+arithmetic is the single-simulation path, so each member must be
+bit-identical to the same simulation stepped alone (tolerance 0).  The
+autotuner only changes tile shapes and the coarse-tail size, which must not
+change a bit either.
+"""
+import numpy as np
+import pytest
+
+from ubootgl_gb300 import workload as WL
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(128, 64), (192, 96), (256, 128), (96, 48), (320, 160), (512, 256)]
+
+
+def build(W, H, seed, precision="fp32", u_in=1.0):
+    from ubootgl_gb300.simulation import Simulation
+    flag = WL.disc_flag(W, H, n_discs=4, seed=seed)
+    vx, vy = WL.initial_velocity(flag, seed=seed + 1, u_in=u_in)
+    sim = Simulation(flag, 1.0, 1e-4)
+    if precision != "fp32":
+        sim.set_options(precision=precision)
+    for n, a in (("vx", vx), ("vy", vy), ("vx_back", vx), ("vy_back", vy)):
+        sim.set(n, a)
+    return sim
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_batch_device_dt_matches_alone(lib, precision):
+    from ubootgl_gb300.simulation import Batch
+    alone = [build(W, H, 10 + i, precision, 0.5 + 0.2 * i) for i, (W, H) in enumerate(SIZES)]
+    members = [build(W, H, 10 + i, precision, 0.5 + 0.2 * i) for i, (W, H) in enumerate(SIZES)]
+    batch = Batch(members)
+    for _ in range(4):
+        for s in alone:
+            s.step_cfl(0.5)
+        batch.step(cfl=0.5)
+    batch.sync()
+    for a, b in zip(alone, members):
+        for n in ("vx", "vy", "vx_back", "vy_back", "p"):
+            assert np.array_equal(a.get(n), b.get(n)), (a.width, n)
+        assert a.last_dt() == b.last_dt()
+    batch.close()
+    for s in alone + members:
+        s.close()
+
+
+def test_batch_host_dt_accum_and_member_steps(lib):
+    """Host time steps, an accumulation applied before a batch step, and
+    members stepped alone between batch steps."""
+    from ubootgl_gb300.simulation import Batch
+    alone = [build(W, H, 30 + i) for i, (W, H) in enumerate(SIZES[:4])]
+    members = [build(W, H, 30 + i) for i, (W, H) in enumerate(SIZES[:4])]
+    batch = Batch(members)
+    rng = np.random.default_rng(3)
+    for it in range(5):
+        dts = np.array([WL.cfl_dt(s.get("vx"), s.get("vy"), s.h) for s in alone], np.float32)
+        if it == 2:
+            for a, b in zip(alone, members):
+                acc = (1e-3 * rng.standard_normal((a.height, a.width - 1))).astype(np.float32)
+                a.set("vx_accum", acc)
+                b.set("vx_accum", acc)
+        if it == 3:
+            for a, b, dt in zip(alone, members, dts):
+                a.step(float(dt))
+                b.step(float(dt))
+            continue
+        for a, dt in zip(alone, dts):
+            a.step(float(dt))
+        batch.step(dts)
+    for a, b in zip(alone, members):
+        for n in ("vx", "vy", "p"):
+            assert np.array_equal(a.get(n), b.get(n)), (a.width, n)
+    batch.close()
+    for s in alone + members:
+        s.close()
+
+
+def test_autotune_bit_identical(lib):
+    a = build(1024, 512, 77)
+    b = build(1024, 512, 77)
+    rep = b.autotune()
+    assert rep["levels"] and "tail_cells" in rep
+    for lv in rep["levels"]:
+        assert lv["pre_us"] > 0 and lv["post_us"] > 0
+    for _ in range(3):
+        a.step_cfl(0.5)
+        b.step_cfl(0.5)
+    for n in ("vx", "vy", "p"):
+        assert np.array_equal(a.get(n), b.get(n)), n
+    a.close()
+    b.close()
+
+
+def test_batch_rejects_tolerance_members(lib):
+    from ubootgl_gb300 import _lib as L
+    from ubootgl_gb300.simulation import Batch
+    s = build(96, 48, 1)
+    s.set_options(solver_mode=L.SOLVE_TOLERANCE, tol=1e-3)
+    b = Batch([s])
+    with pytest.raises(L.UbgError):
+        b.step(cfl=0.5)
+    b.close()
+    s.close()

@@ -1,0 +1,88 @@
+"""The step server: results independent of the mix, admission by budget,
+latency statistics.
+
+Each session's kernels touch only that session's memory and run the
+single-simulation path, so a session stepped among many others must be
+bit-identical (tolerance 0) to the same session stepped alone.
+"""
+import numpy as np
+import pytest
+
+from ubootgl_gb300 import workload as WL
+
+pytestmark = pytest.mark.gpu
+
+
+def session_inputs(W, H, seed, u_in=1.0):
+    flag = WL.disc_flag(W, H, n_discs=4, seed=seed)
+    vx, vy = WL.initial_velocity(flag, seed=seed + 1, u_in=u_in)
+    return flag, vx, vy
+
+
+def test_alone_vs_mixed_bit_identical(lib):
+    from ubootgl_gb300.simulation import Server
+    sizes = [(256, 128), (512, 256), (128, 64), (384, 192), (1024, 512), (192, 96)]
+    rng = np.random.default_rng(0)
+    # alone: one session, its requests one after another
+    target = (300, 150, 41)
+    solo = Server(8 << 30, max_active=4)
+    sid = solo.open(*session_inputs(*target))
+    reqs = [3, 1, 5, 2]
+    for k in reqs:
+        solo.wait(solo.submit(sid, k))
+    alone = {n: solo.get(sid, n) for n in ("vx", "vy", "p")}
+    solo.close()
+    # in a mix: the same session among others, requests interleaved
+    mix = Server(8 << 30, max_active=4)
+    others = [mix.open(*session_inputs(W, H, 50 + i, 0.6 + 0.15 * i))
+              for i, (W, H) in enumerate(sizes)]
+    sid = mix.open(*session_inputs(*target))
+    pending = []
+    for k in reqs:
+        for o in rng.permutation(others)[:4]:
+            pending.append(mix.submit(int(o), int(rng.integers(1, 6))))
+        pending.append(mix.submit(sid, k))
+    for r in pending:
+        mix.wait(r)
+    for n in ("vx", "vy", "p"):
+        assert np.array_equal(mix.get(sid, n), alone[n]), n
+    st = mix.stats()
+    assert st["completed"] == len(pending)
+    assert st["queued"] == 0 and st["active"] == 0
+    assert 0 < st["p50_ms"] <= st["p99_ms"] <= st["max_ms"]
+    mix.close()
+
+
+def test_admission_by_budget(lib):
+    from ubootgl_gb300 import _lib as L
+    from ubootgl_gb300.simulation import Server
+    import ctypes as C
+    b = C.c_size_t()
+    L.check(lib.ubg_device_bytes(512, 256, C.byref(b)))
+    srv = Server(int(2.5 * b.value), max_active=2)
+    ids = [srv.open(*session_inputs(512, 256, s)) for s in range(4)]
+    assert ids[0] is not None and ids[1] is not None
+    assert ids[2] is None and ids[3] is None
+    st = srv.stats()
+    assert st["rejected_sessions"] == 2 and st["sessions"] == 2
+    assert st["device_bytes_used"] <= int(2.5 * b.value)
+    srv.close_session(ids[0])  # memory frees up: a new session is admitted
+    assert srv.open(*session_inputs(512, 256, 9)) is not None
+    srv.close()
+
+
+def test_mixed_precision_sessions(lib):
+    from ubootgl_gb300.simulation import Server
+    srv = Server(8 << 30, max_active=8)
+    a = srv.open(*session_inputs(256, 128, 3), precision="fp16")
+    b = srv.open(*session_inputs(256, 128, 3), precision="fp32")
+    ra, rb = srv.submit(a, 4), srv.submit(b, 4)
+    srv.wait(ra)
+    srv.wait(rb)
+    # same flow, two solvers: the velocities agree to the mixed solver's
+    # accuracy (p itself is fixed only up to a constant by the solver's
+    # singular system, and the two solvers drift differently in it)
+    va, vb = srv.get(a, "vx"), srv.get(b, "vx")
+    assert np.isfinite(srv.get(a, "p")).all()
+    assert np.abs(va - vb).max() <= 5e-3 * np.abs(vb).max()
+    srv.close()

@@ -29,6 +29,14 @@ class Options(C.Structure):
                 ("max_vcycles", C.c_int), ("precision", C.c_int), ("use_graph", C.c_int)]
 
 
+class ServeStats(C.Structure):
+    _fields_ = [("sessions", C.c_int), ("queued", C.c_int), ("active", C.c_int),
+                ("completed", C.c_longlong), ("rejected_sessions", C.c_longlong),
+                ("cell_steps", C.c_longlong), ("device_bytes_used", C.c_size_t),
+                ("busy_ms", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("max_ms", C.c_double)]
+
+
 # name -> (restype, argtypes); every int-returning call is checked
 _P = C.c_void_p
 _FP = C.POINTER(C.c_float)
@@ -53,6 +61,24 @@ _SIGS = {
     "ubg_snapshot_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
     "ubg_snapshot": (C.c_int, [_P, C.c_void_p]),
     "ubg_restore": (C.c_int, [_P, C.c_void_p]),
+    "ubg_autotune": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
+    "ubg_batch_create": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(_P)]),
+    "ubg_batch_destroy": (C.c_int, [_P]),
+    "ubg_batch_step": (C.c_int, [_P, _FP, C.c_float]),
+    "ubg_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "ubg_batch_sync": (C.c_int, [_P]),
+    "ubg_device_bytes": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_size_t)]),
+    "ubg_sim_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
+    "ubg_server_create": (C.c_int, [C.c_size_t, C.c_int, C.POINTER(_P)]),
+    "ubg_server_destroy": (C.c_int, [_P]),
+    "ubg_server_open": (C.c_int, [_P, _FP, C.c_int, C.c_int, C.c_float, C.c_float, _FP, _FP,
+                                  C.POINTER(Options), C.POINTER(C.c_int)]),
+    "ubg_server_close": (C.c_int, [_P, C.c_int]),
+    "ubg_server_submit": (C.c_int, [_P, C.c_int, C.c_int, C.c_float, C.POINTER(C.c_uint64)]),
+    "ubg_server_wait": (C.c_int, [_P, C.c_uint64, C.POINTER(C.c_double)]),
+    "ubg_server_drain": (C.c_int, [_P]),
+    "ubg_server_session_sim": (C.c_int, [_P, C.c_int, C.POINTER(_P)]),
+    "ubg_server_stats": (C.c_int, [_P, C.POINTER(ServeStats)]),
     "ubg_apply_accumulated_velocity": (C.c_int, [_P]),
     "ubg_diffuse": (C.c_int, [_P, C.c_float]),
     "ubg_advect": (C.c_int, [_P, C.c_float]),

@@ -90,6 +90,7 @@ struct ubg_sim {
   ubg_options opt{};
   cudaStream_t st = nullptr;
   void *arena = nullptr;
+  size_t arena_bytes = 0;
   VelBufs v{};
   int fx = 0, fy = 0;
   float *ax = nullptr, *ay = nullptr;
@@ -116,6 +117,7 @@ struct ubg_sim {
   // CUDA graph of the fixed-cycle step body
   cudaGraphExec_t graph = nullptr;
   int graph_key = -1;
+  long gen = 0;  // bumped whenever something baked into a captured step changes
   // profiling
   bool prof = false;
   Profiler profiler;
@@ -514,6 +516,7 @@ int ubg_create(const float *flag, int width, int height, float pwidth, float mu,
     size_t bb = (n + 255) / 256 * 256;
     size_t extra = 256 * 3 + (size_t)kMaxSinks * 9 * sizeof(SinkCell);
     size_t total = 6 * fb + 2 * bb + extra;
+    s->arena_bytes = total;
     if (cudaMalloc(&s->arena, total) != cudaSuccess) {
       cudaGetLastError();
       throw std::bad_alloc();
@@ -584,6 +587,7 @@ int ubg_set_options(ubg_sim *s, const ubg_options *o) {
       mg_low_alloc(s->lo, s->mg, o->precision);
     s->opt = *o;
     s->graph_key = -1;
+    s->gen++;
     return UBG_OK;
   });
 }
@@ -595,6 +599,7 @@ int ubg_set_bcs(ubg_sim *s, int west, int east, int north, int south) {
       if (b < 0 || b > 3) throw ArgError("boundary type");
     s->bc = Bcs{west, east, north, south};
     s->graph_key = -1;  // boundary types are baked into the captured step
+    s->gen++;
     return UBG_OK;
   });
 }
@@ -1346,8 +1351,240 @@ int ubg_restore(ubg_sim *s, const void *src) {
     s->last_dt = hd.last_dt;
     s->accum_dirty = true;
     s->graph_key = -1;
+    s->gen++;
     s->flag_changed();
     s->sync();
+    return UBG_OK;
+  });
+}
+
+// -------------------------------------------------------------- autotuner
+int ubg_autotune(ubg_sim *s, char *report, size_t len) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    s->sync();
+    std::string rep;
+    mg_autotune(s->mg, s->st, &rep);
+    s->graph_key = -1;  // the captured step uses the old tiles
+    s->gen++;
+    if (report && len) {
+      size_t n = std::min(len - 1, rep.size());
+      std::memcpy(report, rep.data(), n);
+      report[n] = 0;
+    }
+    return UBG_OK;
+  });
+}
+
+// ----------------------------------------------------------------- batch
+// Many independent simulations advanced by one graph launch: each member's
+// fixed-cycle step body is captured on its own stream as a parallel branch
+// of one CUDA graph, so the members' kernels run concurrently and the host
+// issues one launch per batch step.
+struct ubg_batch {
+  std::vector<ubg_sim *> sims;
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  std::vector<cudaEvent_t> pre, join;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<long long> key;
+  std::vector<int> after_fx, after_fy, after_cur0;
+  long graph_launches = 0;
+
+  ~ubg_batch() {
+    if (st) cudaStreamSynchronize(st);
+    if (graph) cudaGraphExecDestroy(graph);
+    for (auto e : pre) cudaEventDestroy(e);
+    for (auto e : join) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (done) cudaEventDestroy(done);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  std::vector<long long> make_key(bool device_dt) const {
+    std::vector<long long> k;
+    k.push_back(device_dt);
+    for (auto *s : sims)
+      k.push_back(((long long)s->fx << 2) | (s->fy << 1) | s->mg.cur0 |
+                  ((long long)s->opt.vcycles << 3) | ((long long)s->opt.precision << 24) |
+                  ((long long)s->mg.tail_top << 32));
+    for (auto *s : sims) k.push_back(s->gen);
+    return k;
+  }
+
+  void capture(bool device_dt, float cfl) {
+    if (graph) {
+      cudaGraphExecDestroy(graph);
+      graph = nullptr;
+    }
+    long l0 = g_stats.launches;
+    size_t n = sims.size();
+    after_fx.assign(n, 0);
+    after_fy.assign(n, 0);
+    after_cur0.assign(n, 0);
+    std::vector<int> fx0(n), fy0(n), c00(n);
+    for (size_t i = 0; i < n; i++) {
+      fx0[i] = sims[i]->fx;
+      fy0[i] = sims[i]->fy;
+      c00[i] = sims[i]->mg.cur0;
+    }
+    cudaGraph_t g = nullptr;
+    UBG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      UBG_CUDA(cudaEventRecord(fork, st));
+      for (size_t i = 0; i < n; i++) {
+        ubg_sim *s = sims[i];
+        UBG_CUDA(cudaStreamWaitEvent(s->st, fork, 0));
+        if (device_dt)
+          launch_cfl(s->v, s->fx, s->fy, cfl, s->h, s->mu, s->pwidth, s->d_umax, s->d_sc, s->st,
+                     true);
+        s->step_body(0);
+        UBG_CUDA(cudaEventRecord(join[i], s->st));
+        UBG_CUDA(cudaStreamWaitEvent(st, join[i], 0));
+        after_fx[i] = s->fx;
+        after_fy[i] = s->fy;
+        after_cur0[i] = s->mg.cur0;
+        s->fx = fx0[i];
+        s->fy = fy0[i];
+        s->mg.cur0 = c00[i];
+      }
+    } catch (...) {
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      for (size_t i = 0; i < n; i++) {
+        sims[i]->fx = fx0[i];
+        sims[i]->fy = fy0[i];
+        sims[i]->mg.cur0 = c00[i];
+      }
+      throw;
+    }
+    UBG_CUDA(cudaStreamEndCapture(st, &g));
+    UBG_CUDA(cudaGraphInstantiate(&graph, g, 0));
+    cudaGraphDestroy(g);
+    graph_launches = g_stats.launches - l0;
+    g_stats.launches = l0;
+  }
+
+  void step(const float *dts, float cfl) {
+    bool device_dt = dts == nullptr;
+    for (size_t i = 0; i < sims.size(); i++) {
+      ubg_sim *s = sims[i];
+      if (!s->sinks.empty()) throw ArgError("a member has pending sinks (step it with ubg_step)");
+      if (s->opt.solver_mode != UBG_SOLVE_FIXED) throw ArgError("batch steps need the fixed solver mode");
+      if (s->prof) throw ArgError("a member is profiling");
+      // work outside the graph, on the member's stream
+      bool accum = s->accum_dirty;
+      if (accum) s->apply_accum();
+      if (!device_dt)
+        s->push_scalars(dts[i]);
+      else if (!s->umax_ready || accum)
+        launch_cfl(s->v, s->fx, s->fy, cfl, s->h, s->mu, s->pwidth, s->d_umax, s->d_sc, s->st,
+                   false);
+      UBG_CUDA(cudaEventRecord(pre[i], s->st));
+    }
+    auto k = make_key(device_dt);
+    if (!graph || k != key || cfl_key != cfl) {
+      capture(device_dt, cfl);
+      key = k;
+      cfl_key = cfl;
+    }
+    for (size_t i = 0; i < sims.size(); i++) UBG_CUDA(cudaStreamWaitEvent(st, pre[i], 0));
+    UBG_CUDA(cudaGraphLaunch(graph, st));
+    UBG_CUDA(cudaEventRecord(done, st));
+    for (size_t i = 0; i < sims.size(); i++) {
+      ubg_sim *s = sims[i];
+      UBG_CUDA(cudaStreamWaitEvent(s->st, done, 0));
+      s->fx = after_fx[i];
+      s->fy = after_fy[i];
+      s->mg.cur0 = after_cur0[i];
+      s->umax_ready = true;
+      s->last_vcycles = s->opt.vcycles;
+    }
+    g_stats.launches += graph_launches;
+  }
+  float cfl_key = -1.0f;
+};
+
+int ubg_batch_create(int n, ubg_sim *const *sims, ubg_batch **out) {
+  return guarded([&] {
+    if (n < 1 || !sims || !out) throw ArgError("null argument");
+    std::unique_ptr<ubg_batch> b(new ubg_batch());
+    for (int i = 0; i < n; i++) {
+      if (!sims[i]) throw ArgError("null member");
+      for (int j = 0; j < i; j++)
+        if (sims[j] == sims[i]) throw ArgError("a simulation appears twice in the batch");
+      b->sims.push_back(sims[i]);
+    }
+    UBG_CUDA(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    UBG_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    UBG_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    b->pre.assign(n, nullptr);
+    b->join.assign(n, nullptr);
+    for (int i = 0; i < n; i++) {
+      UBG_CUDA(cudaEventCreateWithFlags(&b->pre[i], cudaEventDisableTiming));
+      UBG_CUDA(cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming));
+    }
+    *out = b.release();
+    return UBG_OK;
+  });
+}
+
+int ubg_batch_destroy(ubg_batch *b) {
+  return guarded([&] {
+    delete b;
+    return UBG_OK;
+  });
+}
+
+int ubg_batch_step(ubg_batch *b, const float *dts, float cfl) {
+  return guarded([&] {
+    if (!b) throw ArgError("null handle");
+    if (!dts && !(cfl > 0.0f)) throw ArgError("cfl must be > 0 when dts is NULL");
+    b->step(dts, cfl);
+    return UBG_OK;
+  });
+}
+
+int ubg_batch_stream(ubg_batch *b, void **stream) {
+  if (!b || !stream) return fail(UBG_EINVAL, "null argument");
+  *stream = (void *)b->st;
+  return UBG_OK;
+}
+
+int ubg_batch_sync(ubg_batch *b) {
+  return guarded([&] {
+    if (!b) throw ArgError("null handle");
+    UBG_CUDA(cudaStreamSynchronize(b->st));
+    return UBG_OK;
+  });
+}
+
+// Device bytes a simulation of this size holds (fields + multigrid), and the
+// bytes a live handle holds now (plus the mixed-precision hierarchy and
+// scratch buffers it allocated).
+static size_t sim_bytes_for(int W, int H) {
+  size_t P = (size_t)round_up(W, 32), n = P * (size_t)H;
+  size_t fb = (n * 4 + 255) / 256 * 256, bb = (n + 255) / 256 * 256;
+  return 6 * fb + 2 * bb + 256 * 3 + (size_t)kMaxSinks * 9 * sizeof(SinkCell) + mg_arena_bytes(W, H);
+}
+
+int ubg_device_bytes(int width, int height, size_t *bytes) {
+  return guarded([&] {
+    if (!bytes || width < 8 || height < 8) throw ArgError("bad argument");
+    *bytes = sim_bytes_for(width, height);
+    return UBG_OK;
+  });
+}
+
+int ubg_sim_device_bytes(ubg_sim *s, size_t *bytes) {
+  return guarded([&] {
+    if (!s || !bytes) throw ArgError("null argument");
+    size_t lo = 0;
+    if (s->lo.levels) {
+      for (auto &L : s->mg.lv) lo += 3 * (((size_t)L.pitch * L.h * 2 + 255) / 256 * 256);
+      lo += ((size_t)s->P * s->H * 4 + 255) / 256 * 256 + 256;
+    }
+    *bytes = s->arena_bytes + s->mg.arena_bytes + lo + s->scratch_bytes;
     return UBG_OK;
   });
 }

@@ -105,6 +105,26 @@ class Simulation:
         L.check(self._lib.ubg_last_dt(self._h, C.byref(v)))
         return v.value
 
+    def autotune(self):
+        """Tunes the multigrid tiles and tail size (extension); returns the
+        report as a dict."""
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        L.check(self._lib.ubg_autotune(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def snapshot(self):
+        """Session state as bytes (ubg_snapshot)."""
+        n = C.c_size_t()
+        L.check(self._lib.ubg_snapshot_bytes(self._h, C.byref(n)))
+        buf = (C.c_char * n.value)()
+        L.check(self._lib.ubg_snapshot(self._h, buf))
+        return bytes(buf)
+
+    def restore(self, blob):
+        buf = C.create_string_buffer(blob, len(blob))
+        L.check(self._lib.ubg_restore(self._h, buf))
+
     def solver_stats(self):
         """(V-cycles or corrections of the last solve, final ||r||/||f|| in
         tolerance mode else -1)."""
@@ -212,6 +232,115 @@ class Simulation:
     flag = property(lambda s: s.get("flag"), lambda s, a: s.set("flag", a))
     vx_current = property(lambda s: s.get("vx_current"))
     vy_current = property(lambda s: s.get("vy_current"))
+
+
+class Batch:
+    """Several simulations advanced by one CUDA graph launch per step
+    (extension).  The members stay usable on their own."""
+
+    def __init__(self, sims):
+        self._lib = L.load()
+        self.sims = list(sims)
+        arr = (C.c_void_p * len(self.sims))(*[s._h.value for s in self.sims])
+        h = C.c_void_p()
+        L.check(self._lib.ubg_batch_create(len(self.sims), arr, C.byref(h)))
+        self._h = h
+
+    def step(self, dts=None, cfl=0.5):
+        if dts is None:
+            L.check(self._lib.ubg_batch_step(self._h, None, cfl))
+        else:
+            d = np.ascontiguousarray(dts, np.float32)
+            assert d.shape == (len(self.sims),)
+            L.check(self._lib.ubg_batch_step(self._h, L.fptr(d), cfl))
+
+    def sync(self):
+        L.check(self._lib.ubg_batch_sync(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ubg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Step server over resident sessions (extension; ubg_server_*)."""
+
+    def __init__(self, budget_bytes, max_active=16):
+        self._lib = L.load()
+        h = C.c_void_p()
+        L.check(self._lib.ubg_server_create(int(budget_bytes), int(max_active), C.byref(h)))
+        self._h = h
+
+    def open(self, flag, vx=None, vy=None, pwidth=1.0, mu=1e-4, precision="fp32", vcycles=2):
+        """Returns the session id, or None when the memory budget rejects it."""
+        flag = _f32(flag)
+        H, W = flag.shape
+        o = L.Options()
+        L.check(self._lib.ubg_default_options(C.byref(o)))
+        o.precision = {"fp32": L.FP32, "fp16": L.MIXED_FP16, "bf16": L.MIXED_BF16}[precision]
+        o.vcycles = vcycles
+        sid = C.c_int()
+        rc = self._lib.ubg_server_open(
+            self._h, L.fptr(flag), W, H, pwidth, mu,
+            None if vx is None else L.fptr(_f32(vx, (H, W - 1))),
+            None if vy is None else L.fptr(_f32(vy, (H - 1, W))), C.byref(o), C.byref(sid))
+        if rc == -6:
+            return None
+        L.check(rc)
+        return sid.value
+
+    def close_session(self, sid):
+        L.check(self._lib.ubg_server_close(self._h, sid))
+
+    def submit(self, sid, steps, cfl=0.5):
+        r = C.c_uint64()
+        L.check(self._lib.ubg_server_submit(self._h, sid, steps, cfl, C.byref(r)))
+        return r.value
+
+    def wait(self, req):
+        ms = C.c_double()
+        L.check(self._lib.ubg_server_wait(self._h, req, C.byref(ms)))
+        return ms.value
+
+    def drain(self):
+        L.check(self._lib.ubg_server_drain(self._h))
+
+    def get(self, sid, name):
+        """A field of an idle session."""
+        h = C.c_void_p()
+        L.check(self._lib.ubg_server_session_sim(self._h, sid, C.byref(h)))
+        view = Simulation.__new__(Simulation)
+        view._lib, view._h = self._lib, h
+        W, H = C.c_int(), C.c_int()
+        # level 0 of the multigrid gives the grid size
+        L.check(self._lib.ubg_mg_level_flag(h, 0, C.byref(W), C.byref(H), None))
+        view.width, view.height = W.value, H.value
+        out = view.get(name)
+        view._h = None
+        return out
+
+    def stats(self):
+        st = L.ServeStats()
+        L.check(self._lib.ubg_server_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in L.ServeStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ubg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Tracers:

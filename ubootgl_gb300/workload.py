@@ -109,3 +109,53 @@ def batch_sizes(n, wmin=128, wmax=2048, seed=0, multiple=32):
     ws = np.exp(rng.uniform(math.log(wmin), math.log(wmax), size=n))
     ws = np.clip((np.round(ws / multiple) * multiple).astype(int), wmin, wmax)
     return [(int(w), int(w) // 2) for w in ws]
+
+
+# ---------------------------------------------------------------------------
+# Many-instance workloads (batched and served simulations).
+
+def log_uniform_widths(n, wmin, wmax, seed, multiple=32):
+    """n widths drawn log-uniform in [wmin, wmax], rounded to `multiple`."""
+    rng = np.random.default_rng(seed)
+    w = np.exp(rng.uniform(math.log(wmin), math.log(wmax), n))
+    return [int(max(wmin, min(wmax, multiple * round(x / multiple)))) for x in w]
+
+
+def fast_velocity(flag, seed=1, amp=0.1, cell=8, u_in=1.0):
+    """Like initial_velocity, with the smoothed noise made by bilinear
+    up-sampling of white noise on a grid `cell` times coarser (a cheap
+    stand-in for the Gaussian filter, for workloads of many instances)."""
+    H, W = flag.shape
+    rng = np.random.default_rng(seed)
+
+    def noise(h, w):
+        ch, cw = h // cell + 2, w // cell + 2
+        c = rng.standard_normal((ch, cw))
+        ys = np.linspace(0, ch - 1.001, h)
+        xs = np.linspace(0, cw - 1.001, w)
+        y0, x0 = ys.astype(int), xs.astype(int)
+        fy, fx = (ys - y0)[:, None], (xs - x0)[None, :]
+        a = c[y0][:, x0] * (1 - fx) + c[y0][:, x0 + 1] * fx
+        b = c[y0 + 1][:, x0] * (1 - fx) + c[y0 + 1][:, x0 + 1] * fx
+        n = a * (1 - fy) + b * fy
+        return (n / max(n.std(), 1e-12)).astype(np.float32)
+
+    vx = (1.0 + amp * noise(H, W - 1)).astype(np.float32)
+    vy = (amp * noise(H - 1, W)).astype(np.float32)
+    vx[:, 0] = u_in
+    vx *= flag[:, :-1] * flag[:, 1:]
+    vy *= flag[:-1, :] * flag[1:, :]
+    vy[0, :] = 0.0
+    return np.ascontiguousarray(vx), np.ascontiguousarray(vy)
+
+
+def instance(W, H, seed, solid_range=(0.08, 0.15), u_in=None):
+    """One instance of a many-instance workload: its own seeded disc mask
+    with a solid fraction drawn from solid_range, its own inflow speed
+    (uniform in [0.5, 1.5] unless given)."""
+    rng = np.random.default_rng(seed)
+    frac = rng.uniform(*solid_range)
+    u = rng.uniform(0.5, 1.5) if u_in is None else u_in
+    flag = disc_flag(W, H, seed=seed + 1, solid_frac=frac)
+    vx, vy = fast_velocity(flag, seed=seed + 2, u_in=u)
+    return flag, vx, vy
