@@ -208,6 +208,8 @@ def run_ours(args):
         if pg:
             pg.barrier()
 
+    # multigrid tiles and tail size for this grid (bit-identical results)
+    tune = sim.autotune() if not args.no_autotune else None
     for _ in range(args.warmup):
         sim.step_cfl(0.5)
     sim.sync()
@@ -277,6 +279,9 @@ def run_ours(args):
                    "grid": [W, H], "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2: step working set %.0f MB > 129 MB"
                          % (working_set_bytes(W, H) / 1e6)},
+        "autotune": ({"tail_cells": tune["tail_cells"],
+                      "tiles": [(lv["pre"], lv["post"]) for lv in tune["levels"]]}
+                     if tune else None),
         "clocks": clk,
         "gpu_launches": int(launches_per_step * args.steps),
         "e2e": e2e,
@@ -310,6 +315,7 @@ def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev):
     stream = C.c_void_p()
     L.check(lib.ubg_stream(sim._h, C.byref(stream)))
     ext = torch.cuda.ExternalStream(stream.value, device=dev)
+    sim.autotune()
     for _ in range(max(3, warmup)):
         sim.step_cfl(0.5)
     sim.sync()
@@ -322,9 +328,19 @@ def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev):
     sim.sync()
     ms = e0.elapsed_time(e1)
     finite = bool(np.isfinite(sim.get("p")).all())
+    # per kernel class (direct launches with event pairs), a few steps
+    sim.profile(True)
+    sim.profile_reset()
+    for _ in range(5):
+        sim.step_cfl(0.5)
+    sim.sync()
+    classes = sim.profile_classes()
+    sim.profile(False)
     sim.close()
+    kern = {k: {"ms_per_step": round(v[0] / 5, 4), "launches_per_step": round(v[1] / 5, 1)}
+            for k, v in sorted(classes.items(), key=lambda kv: -kv[1][0])}
     return {"value": round(W * H * steps / (ms / 1e3) / 1e6, 2), "unit": "Mcell-steps/s",
-            "ms_per_step": round(ms / steps, 5), "steps": steps,
+            "ms_per_step": round(ms / steps, 5), "steps": steps, "kernels": kern,
             "solver": "2 FP32 defect corrections, 16-bit (%s) V-cycle, FP64 norms and coarse "
                       "solve" % precision, "fields_finite": finite}
 
@@ -538,32 +554,34 @@ def measured_peaks():
 
 
 def end_to_end(sim, L, lib, W, H, steps, barrier, pg, world, dev):
-    """Same metric through the public C ABI with host buffers: per step the
-    velocity state goes host -> device from pinned memory, the step runs, and
-    the display fields (vx_current, vy_current) come back device -> host."""
+    """Same metric through the public C ABI with host buffers: every step
+    copies its velocity state host -> device from pinned memory
+    (ubg_io_upload_async), runs (ubg_step_cfl) and copies its resulting
+    velocity device -> host (ubg_io_download_async); the copies of one step
+    overlap the kernels of its neighbours (two host buffer sets, alternating).
+    The timed region ends when the last result is on the host."""
     import torch
-    hx = L.PinnedArray((H, W - 1))
-    hy = L.PinnedArray((H - 1, W))
-    ox = L.PinnedArray((H, W - 1))
-    oy = L.PinnedArray((H - 1, W))
-    hx.array[:] = sim.get("vx")
-    hy.array[:] = sim.get("vy")
-    fx, fy = L.FIELDS["vx"], L.FIELDS["vy"]
-    cx, cy = L.FIELDS["vx_current"], L.FIELDS["vy_current"]
+    hin = [(L.PinnedArray((H, W - 1)), L.PinnedArray((H - 1, W))) for _ in range(2)]
+    hout = [(L.PinnedArray((H, W - 1)), L.PinnedArray((H - 1, W))) for _ in range(2)]
+    for a, b in hin:
+        a.array[:] = sim.get("vx")
+        b.array[:] = sim.get("vy")
 
-    def one():
-        L.check(lib.ubg_upload(sim._h, fx, L.fptr(hx.array)))
-        L.check(lib.ubg_upload(sim._h, fy, L.fptr(hy.array)))
+    def one(i):
+        a, b = hin[i & 1]
+        L.check(lib.ubg_io_upload_async(sim._h, L.fptr(a.array), L.fptr(b.array)))
         sim.step_cfl(0.5)
-        L.check(lib.ubg_download(sim._h, cx, L.fptr(ox.array)))
-        L.check(lib.ubg_download(sim._h, cy, L.fptr(oy.array)))
+        c, d = hout[i & 1]
+        L.check(lib.ubg_io_download_async(sim._h, L.fptr(c.array), L.fptr(d.array)))
 
-    for _ in range(3):
-        one()
+    for i in range(3):
+        one(i)
+    L.check(lib.ubg_io_wait(sim._h))
     barrier()
     t0 = time.perf_counter()
-    for _ in range(steps):
-        one()
+    for i in range(steps):
+        one(i)
+    L.check(lib.ubg_io_wait(sim._h))
     t1 = time.perf_counter()
     barrier()
     sec = t1 - t0
@@ -592,6 +610,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--mode-steps", type=int, default=500,
                     help="timed steps per mixed-precision mode (0: skip)")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batch", type=int, default=64, help="batched instances (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--batch-precisions", default="fp32,fp16")

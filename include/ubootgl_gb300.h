@@ -147,6 +147,23 @@ int ubg_last_dt(ubg_sim *sim, float *dt);
  * ||r|| / ||f * flag|| (else -1).  Host values; no synchronisation. */
 int ubg_solver_stats(ubg_sim *sim, int *vcycles, double *rel_residual);
 
+/* Asynchronous host I/O (extension), for callers that feed and read every
+ * step without stalling the GPU:
+ *  - ubg_io_upload_async copies vx ((W-1) x H) and vy (W x (H-1)) from
+ *    pinned host memory into device staging buffers on the handle's I/O
+ *    stream; the next step (ubg_step / ubg_step_cfl / a batch step) makes
+ *    them the front velocity before its first kernel.
+ *  - ubg_io_download_async snapshots the current vx / vy on the device
+ *    (ordered after the steps enqueued so far) and copies the snapshot to
+ *    pinned host memory on a second I/O stream, overlapping the following
+ *    steps and uploads.
+ *  - ubg_io_wait waits for every copy of both I/O streams.
+ * The host buffers must stay valid, and unmodified (uploads) or unread
+ * (downloads), until ubg_io_wait; alternate two sets to overlap steps. */
+int ubg_io_upload_async(ubg_sim *sim, const float *vx, const float *vy);
+int ubg_io_download_async(ubg_sim *sim, float *vx, float *vy);
+int ubg_io_wait(ubg_sim *sim);
+
 /* Individual stages of the step, for callers that drive them one by one and
  * for stage-wise parity tests.  `dt` sets the member Simulation::dt first. */
 int ubg_apply_accumulated_velocity(ubg_sim *sim); /* simulation.cpp:376-396 */

@@ -84,9 +84,8 @@ def test_autotune_bit_identical(lib):
     a = build(1024, 512, 77)
     b = build(1024, 512, 77)
     rep = b.autotune()
-    assert rep["levels"] and "tail_cells" in rep
-    for lv in rep["levels"]:
-        assert lv["pre_us"] > 0 and lv["post_us"] > 0
+    assert rep["levels"] and "tail_cells" in rep and rep["vcycle_us"] > 0
+    assert all(t["vcycle_us"] > 0 for t in rep["trials"])
     for _ in range(3):
         a.step_cfl(0.5)
         b.step_cfl(0.5)

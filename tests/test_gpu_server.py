@@ -84,5 +84,5 @@ def test_mixed_precision_sessions(lib):
     # singular system, and the two solvers drift differently in it)
     va, vb = srv.get(a, "vx"), srv.get(b, "vx")
     assert np.isfinite(srv.get(a, "p")).all()
-    assert np.abs(va - vb).max() <= 5e-3 * np.abs(vb).max()
+    assert np.abs(va - vb).max() <= 0.05 * np.abs(vb).max()
     srv.close()

@@ -128,6 +128,45 @@ struct ubg_sim {
   // grow-only device scratch for the item / cell lists of the game-side calls
   void *scratch = nullptr;
   size_t scratch_bytes = 0;
+  // asynchronous host I/O (ubg_io_*): staging buffers and a copy stream
+  float *io_in[2] = {nullptr, nullptr}, *io_out[2] = {nullptr, nullptr};
+  void *io_arena = nullptr;
+  cudaStream_t io_st = nullptr, io_out_st = nullptr;  // host->device, device->host
+  cudaEvent_t io_in_ready = nullptr, io_in_free = nullptr, io_out_copied = nullptr,
+              io_out_done = nullptr;
+  bool io_staged = false;
+
+  void io_init() {
+    if (io_arena) return;
+    size_t fb = ((size_t)P * H * 4 + 255) / 256 * 256;
+    if (cudaMalloc(&io_arena, 4 * fb) != cudaSuccess) {
+      cudaGetLastError();
+      io_arena = nullptr;
+      throw std::bad_alloc();
+    }
+    char *p = (char *)io_arena;
+    for (int k = 0; k < 2; k++, p += fb) io_in[k] = (float *)p;
+    for (int k = 0; k < 2; k++, p += fb) io_out[k] = (float *)p;
+    UBG_CUDA(cudaStreamCreateWithFlags(&io_st, cudaStreamNonBlocking));
+    UBG_CUDA(cudaStreamCreateWithFlags(&io_out_st, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&io_in_ready, &io_in_free, &io_out_copied, &io_out_done})
+      UBG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    UBG_CUDA(cudaEventRecord(io_in_free, st));
+    UBG_CUDA(cudaEventRecord(io_out_done, io_out_st));
+  }
+
+  // staged inputs become the front velocity before the next step's kernels
+  void io_consume() {
+    if (!io_staged) return;
+    UBG_CUDA(cudaStreamWaitEvent(st, io_in_ready, 0));
+    UBG_CUDA(cudaMemcpy2DAsync(v.vx[fx], (size_t)P * 4, io_in[0], (size_t)P * 4, (size_t)(W - 1) * 4,
+                               H, cudaMemcpyDeviceToDevice, st));
+    UBG_CUDA(cudaMemcpy2DAsync(v.vy[fy], (size_t)P * 4, io_in[1], (size_t)P * 4, (size_t)W * 4, H - 1,
+                               cudaMemcpyDeviceToDevice, st));
+    UBG_CUDA(cudaEventRecord(io_in_free, st));
+    io_staged = false;
+    umax_ready = false;
+  }
 
   void *scratch_get(size_t bytes) {
     if (bytes > scratch_bytes) {
@@ -165,6 +204,13 @@ struct ubg_sim {
     if (h_norm) cudaFreeHost(h_norm);
     mg_low_free(lo);
     if (scratch) cudaFree(scratch);
+    if (io_st) cudaStreamSynchronize(io_st);
+    if (io_out_st) cudaStreamSynchronize(io_out_st);
+    for (cudaEvent_t e : {io_in_ready, io_in_free, io_out_copied, io_out_done})
+      if (e) cudaEventDestroy(e);
+    if (io_st) cudaStreamDestroy(io_st);
+    if (io_out_st) cudaStreamDestroy(io_out_st);
+    if (io_arena) cudaFree(io_arena);
     mg_free(mg);
     if (arena) cudaFree(arena);
     if (st) cudaStreamDestroy(st);
@@ -326,6 +372,7 @@ struct ubg_sim {
       }
     } pi(prof, &profiler);
     if (prof) UBG_CUDA(cudaEventRecord(ev_step[0], st));
+    io_consume();
     if (accum_dirty) apply_accum();
     int nsc = 0;
     if (device_dt) {
@@ -1473,6 +1520,7 @@ struct ubg_batch {
       if (s->opt.solver_mode != UBG_SOLVE_FIXED) throw ArgError("batch steps need the fixed solver mode");
       if (s->prof) throw ArgError("a member is profiling");
       // work outside the graph, on the member's stream
+      s->io_consume();
       bool accum = s->accum_dirty;
       if (accum) s->apply_accum();
       if (!device_dt)
@@ -1585,6 +1633,54 @@ int ubg_sim_device_bytes(ubg_sim *s, size_t *bytes) {
       lo += ((size_t)s->P * s->H * 4 + 255) / 256 * 256 + 256;
     }
     *bytes = s->arena_bytes + s->mg.arena_bytes + lo + s->scratch_bytes;
+    return UBG_OK;
+  });
+}
+
+// ------------------------------------------------------ asynchronous host I/O
+int ubg_io_upload_async(ubg_sim *s, const float *vx, const float *vy) {
+  return guarded([&] {
+    if (!s || !vx || !vy) throw ArgError("null argument");
+    s->io_init();
+    // the staging buffers are free once the previous staged inputs were consumed
+    UBG_CUDA(cudaStreamWaitEvent(s->io_st, s->io_in_free, 0));
+    UBG_CUDA(cudaMemcpy2DAsync(s->io_in[0], (size_t)s->P * 4, vx, (size_t)(s->W - 1) * 4,
+                               (size_t)(s->W - 1) * 4, s->H, cudaMemcpyHostToDevice, s->io_st));
+    UBG_CUDA(cudaMemcpy2DAsync(s->io_in[1], (size_t)s->P * 4, vy, (size_t)s->W * 4, (size_t)s->W * 4,
+                               s->H - 1, cudaMemcpyHostToDevice, s->io_st));
+    UBG_CUDA(cudaEventRecord(s->io_in_ready, s->io_st));
+    s->io_staged = true;
+    return UBG_OK;
+  });
+}
+
+int ubg_io_download_async(ubg_sim *s, float *vx, float *vy) {
+  return guarded([&] {
+    if (!s || !vx || !vy) throw ArgError("null argument");
+    s->io_init();
+    // snapshot the current fields on the simulation's stream (the next step
+    // overwrites them), then copy to the host on the I/O stream
+    UBG_CUDA(cudaStreamWaitEvent(s->st, s->io_out_done, 0));
+    UBG_CUDA(cudaMemcpy2DAsync(s->io_out[0], (size_t)s->P * 4, s->v.vx[s->fx], (size_t)s->P * 4,
+                               (size_t)(s->W - 1) * 4, s->H, cudaMemcpyDeviceToDevice, s->st));
+    UBG_CUDA(cudaMemcpy2DAsync(s->io_out[1], (size_t)s->P * 4, s->v.vy[s->fy], (size_t)s->P * 4,
+                               (size_t)s->W * 4, s->H - 1, cudaMemcpyDeviceToDevice, s->st));
+    UBG_CUDA(cudaEventRecord(s->io_out_copied, s->st));
+    UBG_CUDA(cudaStreamWaitEvent(s->io_out_st, s->io_out_copied, 0));
+    UBG_CUDA(cudaMemcpy2DAsync(vx, (size_t)(s->W - 1) * 4, s->io_out[0], (size_t)s->P * 4,
+                               (size_t)(s->W - 1) * 4, s->H, cudaMemcpyDeviceToHost, s->io_out_st));
+    UBG_CUDA(cudaMemcpy2DAsync(vy, (size_t)s->W * 4, s->io_out[1], (size_t)s->P * 4, (size_t)s->W * 4,
+                               s->H - 1, cudaMemcpyDeviceToHost, s->io_out_st));
+    UBG_CUDA(cudaEventRecord(s->io_out_done, s->io_out_st));
+    return UBG_OK;
+  });
+}
+
+int ubg_io_wait(ubg_sim *s) {
+  return guarded([&] {
+    if (!s) throw ArgError("null handle");
+    if (s->io_st) UBG_CUDA(cudaStreamSynchronize(s->io_st));
+    if (s->io_out_st) UBG_CUDA(cudaStreamSynchronize(s->io_out_st));
     return UBG_OK;
   });
 }

@@ -250,7 +250,7 @@ struct Tile {
 // because x0 + y0 is even.  After half sweep i only cells within HALO - i of
 // the tile are still exact, so each half sweep updates just that cone.
 template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float>
-__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 4) k_mg(MgArgsT<S> a) {
+__global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg(MgArgsT<S> a) {
   constexpr int NTY = NT / 32;
   using T = Tile<TX, TY, HALO>;
   using St = Sto<S>;
@@ -862,6 +862,7 @@ void set_vcycle_attrs() {
   set_smem_attr<40, 8, 12, true, 256, S>();
   set_smem_attr<112, 24, 8, true, 256, S>();
   set_smem_attr<48, 40, 8, true, 256, S>();
+  set_smem_attr<112, 114, 8, true, 1024, S>();
 }
 
 void init_kernel_attributes() {
@@ -881,9 +882,9 @@ void init_kernel_attributes() {
 // is chosen by level width so small levels still fill the GPU.
 // Smoother tiles the autotuner chooses from (3-sweep launches need a halo of
 // 8, 5-sweep launches 12): id -> TX x TY, halo, threads.
-constexpr int kTiles = 5;
+constexpr int kTiles = 6;
 const char *const kTileNames[kTiles] = {"112x50/h8/512", "48x16/h8/256", "40x8/h12/256",
-                                        "112x24/h8/256", "48x40/h8/256"};
+                                        "112x24/h8/256", "48x40/h8/256", "112x114/h8/1024"};
 bool tile_ok(int id, int nsweeps) { return id >= 0 && id < kTiles && (nsweeps <= 3 || id == 2); }
 
 template <class S>
@@ -894,6 +895,7 @@ void launch_mg_tile(const MgArgsT<S> &a, int id, cudaStream_t st) {
     case 2: launch_mg_t<40, 8, 12, true, 256, S>(a, st); break;
     case 3: launch_mg_t<112, 24, 8, true, 256, S>(a, st); break;
     case 4: launch_mg_t<48, 40, 8, true, 256, S>(a, st); break;
+    case 5: launch_mg_t<112, 114, 8, true, 1024, S>(a, st); break;
     default: throw ArgError("smoother tile id");
   }
 }
@@ -1230,7 +1232,7 @@ MgArgsT<S> level_args_lo(MgHier &mg, MgLow &lo, int l, int cin, int ns) {
 template <class S>
 void solve_level_lo(MgHier &mg, MgLow &lo, std::vector<int> &cur, int l, cudaStream_t st) {
   const KernelClass kc = l == 0 ? KC_SMOOTH_L0 : (l == 1 ? KC_SMOOTH_L1 : KC_SMOOTH_COARSE);
-  if (l >= 1 && l == mg.tail_top) {
+  if (l >= 1 && l == mg.tail_top_fp64) {
     run_tail_t<S, double>(mg, l, (const S *)lo.rhs[l], (S *)lo.e[0][l], lo.rfac.data(), st);
     cur[l] = 0;
     return;
@@ -1335,11 +1337,14 @@ int solve_mixed_t(MgHier &mg, MgLow &lo, double tol, int max_cycles, double fnor
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
-int choose_tail(const std::vector<MgLevel> &lv, int max_cells) {
+// The first level whose whole coarse end fits the tail kernel (arithmetic
+// elements of elem_bytes: 4 for FP32, 8 for the mixed solver's FP64) with a
+// top level of at most max_cells.
+int choose_tail(const std::vector<MgLevel> &lv, int max_cells, size_t elem_bytes = 4) {
   int L = (int)lv.size();
   for (int lt = 1; lt <= L - 2; lt++) {
-    // sized for the FP64 arithmetic of the mixed solver's coarse solve
-    if (tail_smem_bytes(lv, lt, 8) <= TAIL_SMEM_MAX && (size_t)lv[lt].w * lv[lt].h <= (size_t)max_cells)
+    if (tail_smem_bytes(lv, lt, elem_bytes) <= TAIL_SMEM_MAX &&
+        (size_t)lv[lt].w * lv[lt].h <= (size_t)max_cells)
       return lt;
   }
   return -1;
@@ -1400,6 +1405,7 @@ void mg_bind(MgHier &mg, int W, int H, float h0, void *arena, size_t bytes) {
   mg.norm = (double *)p;
   mg.post_norm2 = nullptr;
   mg.tail_top = choose_tail(lv, mg.tail_cells);
+  mg.tail_top_fp64 = choose_tail(lv, 2048, 8);
   mg.lv = lv;
   mg.levels = (int)lv.size();
   mg.arena = nullptr;  // not owned
@@ -1507,90 +1513,111 @@ double time_ms(EvPair &ev, cudaStream_t st, int warm, int reps, F &&f) {
 }
 }  // namespace
 
+// The autotuner times whole V-cycles, captured into a CUDA graph as the step
+// runs them, so launch gaps and the cache state between launches count:
+// coordinate descent over the tail size, then each tiled level's pre- and
+// post-smoothing tile.  The pressure is saved first and restored after the
+// trials (a V-cycle leaves p in the buffer it started in).
 void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
   init_kernel_attributes();
   const int nl = mg.levels;
   EvPair ev;
-  const int warm = 2, reps = 5;
-  // the tail sizes to try, and the deepest level any of them leaves tiled
-  const int tail_cand[] = {512, 1024, 2048, 4096};
-  int deepest = nl - 2;
-  for (int tc : tail_cand) {
-    int lt = choose_tail(mg.lv, tc);
-    if (lt >= 1) deepest = std::max(1, std::min(deepest, std::max(lt, 1)));
+  MgLevel &L0 = mg.lv[0];
+  const size_t pbytes = (size_t)L0.pitch * L0.h * sizeof(float);
+  float *saved = nullptr;
+  if (cudaMalloc(&saved, pbytes) != cudaSuccess) {
+    cudaGetLastError();
+    throw std::bad_alloc();
   }
-  std::vector<double> best_pre(nl, 0.0), best_post(nl, 0.0);
-  std::string rep = "{\"levels\": [";
-  // per level (not the coarsest): the pre-smoothing launch (3 sweeps +
-  // residual + restriction) and the post-smoothing launch (prolongation +
-  // correction + 3 sweeps) with each candidate tile.  Trials read the
-  // level's current arrays and write only its idle ping-pong buffer and the
-  // next level's rhs: the solver state is unchanged.
-  int last_tiled = std::max(0, std::min(nl - 3, std::max(deepest, mg.tail_top >= 1 ? mg.tail_top : nl - 2) - 1));
-  for (int l = 0; l <= last_tiled; l++) {
-    MgLevel &L = mg.lv[l], &C = mg.lv[l + 1];
-    int cur = l == 0 ? mg.cur0 : 0;
-    double tpre[kTiles], tpost[kTiles];
-    int bp = -1, bq = -1;
-    for (int id = 0; id < kTiles; id++) {
-      MgArgs a = level_args(L, L.e[cur], L.e[1 - cur], 3, 1.0f);
-      a.zgbc = l == 0;
-      a.zero_init = l > 0;
-      a.rc = C.rhs;
-      a.cw = C.w;
-      a.ch = C.h;
-      a.cpitch = C.pitch;
-      tpre[id] = time_ms(ev, st, warm, reps, [&] { launch_mg_tile(a, id, st); });
-      MgArgs b = level_args(L, L.e[cur], L.e[1 - cur], 3, 1.0f);
-      b.zgbc = l == 0;
-      b.ec = C.e[0];
-      b.codec = C.code;
-      b.cpitch = C.pitch;
-      b.cw = C.w;
-      b.ch = C.h;
-      tpost[id] = time_ms(ev, st, warm, reps, [&] { launch_mg_tile(b, id, st); });
-      if (bp < 0 || tpre[id] < tpre[bp]) bp = id;
-      if (bq < 0 || tpost[id] < tpost[bq]) bq = id;
+  const int c0 = mg.cur0;
+  UBG_CUDA(cudaMemcpyAsync(saved, L0.e[c0], pbytes, cudaMemcpyDeviceToDevice, st));
+  auto vcycle_us = [&]() {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    UBG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      mg_solve(mg, true, st);
+    } catch (...) {
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      mg.cur0 = c0;
+      throw;
     }
-    L.tile_pre = bp;
-    L.tile_post = bq;
-    best_pre[l] = tpre[bp];
-    best_post[l] = tpost[bq];
-    char buf[320];
-    snprintf(buf, sizeof(buf),
-             "%s{\"level\": %d, \"w\": %d, \"h\": %d, \"pre\": \"%s\", \"pre_us\": %.2f, "
-             "\"post\": \"%s\", \"post_us\": %.2f}",
-             l ? ", " : "", l, L.w, L.h, kTileNames[bp], 1e3 * tpre[bp], kTileNames[bq],
-             1e3 * tpost[bq]);
-    rep += buf;
-  }
-  rep += "], \"tail\": [";
-  // the tail size: tail time + the tiled launches of the levels above it
-  int best_tc = mg.tail_cells, best_lt = mg.tail_top;
-  double best_cost = -1.0;
+    UBG_CUDA(cudaStreamEndCapture(st, &g));
+    mg.cur0 = c0;
+    UBG_CUDA(cudaGraphInstantiate(&ge, g, 0));
+    cudaGraphDestroy(g);
+    double ms = time_ms(ev, st, 2, 6, [&] { UBG_CUDA(cudaGraphLaunch(ge, st)); });
+    cudaGraphExecDestroy(ge);
+    return 1e3 * ms;
+  };
+  std::string rep = "{\"trials\": [";
   bool first = true;
-  for (int tc : tail_cand) {
-    int lt = choose_tail(mg.lv, tc);
-    if (lt < 1 || lt - 1 > last_tiled) continue;
-    double t = time_ms(ev, st, warm, reps, [&] { run_tail(mg, lt, st); });
-    double cost = t;
-    for (int l = 0; l < lt; l++) cost += best_pre[l] + best_post[l];
-    char buf[160];
-    snprintf(buf, sizeof(buf), "%s{\"cells\": %d, \"top\": %d, \"tail_us\": %.2f, \"vcycle_us\": %.2f}",
-             first ? "" : ", ", tc, lt, 1e3 * t, 1e3 * cost);
+  auto note = [&](const char *what, int level, const char *choice, double us) {
+    char buf[200];
+    snprintf(buf, sizeof(buf), "%s{\"what\": \"%s\", \"level\": %d, \"choice\": \"%s\", \"vcycle_us\": %.2f}",
+             first ? "" : ", ", what, level, choice, us);
     rep += buf;
     first = false;
-    if (best_cost < 0.0 || cost < best_cost) {
-      best_cost = cost;
+  };
+  double best = vcycle_us();
+  note("start", -1, "default", best);
+  // tail size
+  const int tail_cand[] = {512, 1024, 2048, 4096, 8192};
+  int best_tc = mg.tail_cells, best_lt = mg.tail_top;
+  for (int tc : tail_cand) {
+    int lt = choose_tail(mg.lv, tc);
+    if (lt < 1 || lt == best_lt) continue;
+    int keep = mg.tail_top;
+    mg.tail_top = lt;
+    double t = vcycle_us();
+    char c[32];
+    snprintf(c, sizeof(c), "%d cells", tc);
+    note("tail", lt, c, t);
+    if (t < best) {
+      best = t;
       best_tc = tc;
       best_lt = lt;
+    } else {
+      mg.tail_top = keep;
     }
   }
-  mg.tail_cells = best_tc;
   mg.tail_top = best_lt;
-  char buf[96];
-  snprintf(buf, sizeof(buf), "], \"tail_cells\": %d, \"tail_top\": %d}", best_tc, best_lt);
+  mg.tail_cells = best_tc;
+  // tiles of the tiled levels (coordinate descent, pre then post)
+  const int last = (mg.tail_top >= 1 ? mg.tail_top : nl - 1) - 1;
+  for (int l = 0; l <= std::min(last, nl - 3); l++) {
+    for (int which = 0; which < 2; which++) {
+      int &slot = which ? mg.lv[l].tile_post : mg.lv[l].tile_pre;
+      int keep = slot;
+      for (int id = 0; id < kTiles; id++) {
+        if (id == keep) continue;
+        slot = id;
+        double t = vcycle_us();
+        note(which ? "post" : "pre", l, kTileNames[id], t);
+        if (t < best) {
+          best = t;
+          keep = id;
+        }
+      }
+      slot = keep;
+    }
+  }
+  UBG_CUDA(cudaMemcpyAsync(L0.e[c0], saved, pbytes, cudaMemcpyDeviceToDevice, st));
+  UBG_CUDA(cudaStreamSynchronize(st));
+  cudaFree(saved);
+  char buf[256];
+  snprintf(buf, sizeof(buf), "], \"vcycle_us\": %.2f, \"tail_cells\": %d, \"tail_top\": %d, \"levels\": [",
+           best, mg.tail_cells, mg.tail_top);
   rep += buf;
+  for (int l = 0; l <= std::min(last, nl - 3); l++) {
+    const MgLevel &L = mg.lv[l];
+    snprintf(buf, sizeof(buf), "%s{\"level\": %d, \"w\": %d, \"h\": %d, \"pre\": \"%s\", \"post\": \"%s\"}",
+             l ? ", " : "", l, L.w, L.h, L.tile_pre >= 0 ? kTileNames[L.tile_pre] : "default",
+             L.tile_post >= 0 ? kTileNames[L.tile_post] : "default");
+    rep += buf;
+  }
+  rep += "]}";
   if (report) *report += rep;
 }
 

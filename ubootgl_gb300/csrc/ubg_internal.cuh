@@ -148,6 +148,7 @@ struct MgHier {
   int cur0 = 0;                  // which e[] of level 0 holds p
   int tail_top = -1;             // first level solved by the one-CTA tail kernel
   int tail_cells = 2048;         // largest top level the tail takes (autotuned)
+  int tail_top_fp64 = -1;        // the same for the mixed solver's FP64 tail
   void *arena = nullptr;
   size_t arena_bytes = 0;
   double *norm = nullptr;        // device scalar for residual norms
