@@ -254,6 +254,13 @@ int ubg_batch_sync(ubg_batch *batch);
 int ubg_device_bytes(int width, int height, size_t *bytes);
 int ubg_sim_device_bytes(ubg_sim *sim, size_t *bytes);
 
+/* Diagnostic (no counterpart in the reference): the kernels replace a
+ * division x / d by a constant d > 0 with Markstein's correction of
+ * x * RN(1/d) (exact for |x| in [2^-100, 2^100], the division otherwise).
+ * This compares the two bit for bit on the device for the n host values x
+ * and writes the number of differences (0 expected). */
+int ubg_selftest_div(const float *x, int n, float d, unsigned *mismatches);
+
 /* ------------------------------------------------------------ step server */
 
 /* Step server (extension): continuous batching of step requests over

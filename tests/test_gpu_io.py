@@ -39,3 +39,20 @@ def test_async_io_pipeline_matches_sync(lib):
         assert np.array_equal(hout[i][1].array, want[i][1]), i
     ref.close()
     sim.close()
+
+
+@pytest.mark.parametrize("d", [1.0001, 2.0001, 3.0, 3.0001, 4.0001, 1.00020003, 1.37, 4.999])
+def test_division_by_reciprocal_exact(lib, d):
+    """The kernels' x / d (Markstein's correction of x * RN(1/d)) equals
+    CUDA's IEEE division bit for bit: random bit patterns over every
+    exponent (zeros, subnormals, infinities, NaNs included)."""
+    import ctypes as C
+    from ubootgl_gb300 import _lib as L
+    rng = np.random.default_rng(int(d * 1000))
+    x = rng.integers(0, 2 ** 32, 1 << 22, dtype=np.uint64).astype(np.uint32).view(np.float32)
+    x = np.concatenate([x, np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-45, -1e-38,
+                                     3.4e38, 1.0, -1.0], np.float32)])
+    bad = C.c_uint()
+    L.check(lib.ubg_selftest_div(L.fptr(np.ascontiguousarray(x)), len(x), np.float32(d),
+                                 C.byref(bad)))
+    assert bad.value == 0

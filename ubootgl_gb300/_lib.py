@@ -70,6 +70,7 @@ _SIGS = {
     "ubg_io_upload_async": (C.c_int, [_P, _FP, _FP]),
     "ubg_io_download_async": (C.c_int, [_P, _FP, _FP]),
     "ubg_io_wait": (C.c_int, [_P]),
+    "ubg_selftest_div": (C.c_int, [_FP, C.c_int, C.c_float, C.POINTER(C.c_uint)]),
     "ubg_device_bytes": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_size_t)]),
     "ubg_sim_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
     "ubg_server_create": (C.c_int, [C.c_size_t, C.c_int, C.POINTER(_P)]),

@@ -71,6 +71,7 @@ StepScalars make_scalars(float dt, float mu, float pwidth, int W, float h) {
   s.dt = dt;
   s.a = dt * mu * ((float)W - 1.0f) / pwidth;
   s.den = 1.0f + 4.0f * s.a;
+  s.rden = 1.0f / s.den;
   s.ih = 1.0f / h;
   s.chalf = 0.5f * dt * s.ih;
   s.cfull = dt * s.ih;
@@ -1681,6 +1682,14 @@ int ubg_io_wait(ubg_sim *s) {
     if (!s) throw ArgError("null handle");
     if (s->io_st) UBG_CUDA(cudaStreamSynchronize(s->io_st));
     if (s->io_out_st) UBG_CUDA(cudaStreamSynchronize(s->io_out_st));
+    return UBG_OK;
+  });
+}
+
+int ubg_selftest_div(const float *x, int n, float d, unsigned *mismatches) {
+  return guarded([&] {
+    if (!x || n < 1 || !mismatches || !(d > 0.0f)) throw ArgError("bad argument");
+    selftest_div_rn(x, n, d, mismatches);
     return UBG_OK;
   });
 }

@@ -182,3 +182,30 @@ void launch_shift_map(VelBufs &v, int fx, int fy, const float *p_in, float *p_ou
 }
 
 }  // namespace ubg
+
+// ------------------------------------------------------------ self-test
+namespace ubg {
+namespace {
+__global__ void k_div_check(const float *x, int n, float d, float r, unsigned *bad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float a = div_rn(x[i], d, r), b = x[i] / d;
+  if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b)) atomicAdd(bad, 1u);
+}
+}  // namespace
+
+int selftest_div_rn(const float *x, int n, float d, unsigned *mismatches) {
+  float *dx = nullptr;
+  unsigned *dbad = nullptr;
+  UBG_CUDA(cudaMalloc(&dx, (size_t)n * sizeof(float)));
+  UBG_CUDA(cudaMalloc(&dbad, sizeof(unsigned)));
+  UBG_CUDA(cudaMemcpy(dx, x, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+  UBG_CUDA(cudaMemset(dbad, 0, sizeof(unsigned)));
+  k_div_check<<<(n + 255) / 256, 256>>>(dx, n, d, 1.0f / d, dbad);
+  UBG_LAUNCH_CHECK();
+  UBG_CUDA(cudaMemcpy(mismatches, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  cudaFree(dx);
+  cudaFree(dbad);
+  return 0;
+}
+}  // namespace ubg

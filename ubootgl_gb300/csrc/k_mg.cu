@@ -61,6 +61,10 @@ __global__ void k_make_code(const uint8_t *__restrict__ flag, uint8_t *code, int
 // at +0 and never becomes -0), val/sum is exact as a multiplication for
 // sum = 1, 2, 4 and a true division for sum = 3, and flag*val equals
 // flag ? val : 0 up to the sign of a zero.
+// x / 3 (correctly rounded either way)
+__device__ __forceinline__ float div3(float x) { return div_rn(x, 3.0f, 1.0f / 3.0f); }
+__device__ __forceinline__ double div3(double x) { return x / 3.0; }
+
 // T = float is the reference's arithmetic; T = double serves the FP64
 // coarse solve of the mixed-precision solver.
 template <class T>
@@ -73,7 +77,7 @@ __device__ __forceinline__ T rb_update1(unsigned c, T pw, T pe, T ps, T pn, T f,
   val = val + f * hh * hh;
   int s = __popc((c >> 1) & 15u);
   if (s == 3)
-    val = val / T(3);
+    val = div3(val);
   else
     val = val * (s == 4 ? T(0.25) : (s == 2 ? T(0.5) : (s == 1 ? T(1) : T(0))));
   if (s == 0) val = T(0);
@@ -217,7 +221,8 @@ struct MgArgsT {
   const S *ec;
   const uint8_t *codec;
   int cpitch;
-  float wsum[5];  // (float)((double)k + 0.0001)
+  float wsum[5];   // (float)((double)k + 0.0001)
+  float rwsum[5];  // RN(1 / wsum[k]), for div_rn
   // epilogue: rc = restrict(residual) (pre-smoothing)
   S *rc;
   int cw, ch;
@@ -372,13 +377,16 @@ __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg
           if (!xo && !yo) {
             ev = E(0);
           } else if (xo && !yo) {
-            ev = (gx >= w - 2) ? 0.0f : (E(0) + E(1)) / a.wsum[F[0] + F[1]];
+            const int k = F[0] + F[1];
+            ev = (gx >= w - 2) ? 0.0f : div_rn(E(0) + E(1), a.wsum[k], a.rwsum[k]);
           } else if (!xo && yo) {
-            ev = (gy >= h - 2) ? 0.0f : (E(0) + E(CW)) / a.wsum[F[0] + F[CW]];
+            const int k = F[0] + F[CW];
+            ev = (gy >= h - 2) ? 0.0f : div_rn(E(0) + E(CW), a.wsum[k], a.rwsum[k]);
           } else {
+            const int k = F[0] + F[CW + 1] + F[1] + F[CW];
             ev = (gx >= w - 2 || gy >= h - 2)
                      ? 0.0f
-                     : (((E(0) + E(CW + 1)) + E(1)) + E(CW)) / a.wsum[F[0] + F[CW + 1] + F[1] + F[CW]];
+                     : div_rn(((E(0) + E(CW + 1)) + E(1)) + E(CW), a.wsum[k], a.rwsum[k]);
           }
           sp[i] = St::fromf(St::tof(sp[i]) + ev);
         }
@@ -672,6 +680,7 @@ struct TailArgs {
   int e_pitch;
   int float_words;  // elements of the arithmetic part of shared memory
   float wsum[5];
+  float rwsum[5];  // RN(1 / wsum[k])
 };
 
 // A level may be worked by a team of threads (a prefix of the block, with
@@ -697,9 +706,18 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs<S> a) {
   uint8_t *bm = smem_raw + (size_t)a.float_words * sizeof(T);
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
   const int nl = a.nlev;
-  const T ws0 = a.wsum[0], ws1 = a.wsum[1], ws2 = a.wsum[2], ws3 = a.wsum[3], ws4 = a.wsum[4];
-  auto WS = [&](int k) {
-    return k == 0 ? ws0 : (k == 1 ? ws1 : (k == 2 ? ws2 : (k == 3 ? ws3 : ws4)));
+  const float ws0 = a.wsum[0], ws1 = a.wsum[1], ws2 = a.wsum[2], ws3 = a.wsum[3], ws4 = a.wsum[4];
+  const float rw0 = a.rwsum[0], rw1 = a.rwsum[1], rw2 = a.rwsum[2], rw3 = a.rwsum[3],
+              rw4 = a.rwsum[4];
+  // x / wsum[k], correctly rounded (div_rn for float, the division for double)
+  auto DIVW = [&](T x, int k) -> T {
+    const float d = k == 0 ? ws0 : (k == 1 ? ws1 : (k == 2 ? ws2 : (k == 3 ? ws3 : ws4)));
+    if constexpr (std::is_same<T, float>::value) {
+      const float r = k == 0 ? rw0 : (k == 1 ? rw1 : (k == 2 ? rw2 : (k == 3 ? rw3 : rw4)));
+      return div_rn(x, d, r);
+    } else {
+      return x / (T)d;
+    }
   };
   auto team_of = [&](int t) {
     (void)t;
@@ -807,14 +825,14 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs<S> a) {
         if (!xo && !yo)
           ev = E(cx, cy);
         else if (xo && !yo)
-          ev = (x >= L.w - 2) ? T(0) : (E(cx, cy) + E(cx + 1, cy)) / WS(F(cx, cy) + F(cx + 1, cy));
+          ev = (x >= L.w - 2) ? T(0) : DIVW(E(cx, cy) + E(cx + 1, cy), F(cx, cy) + F(cx + 1, cy));
         else if (!xo && yo)
-          ev = (y >= L.h - 2) ? T(0) : (E(cx, cy) + E(cx, cy + 1)) / WS(F(cx, cy) + F(cx, cy + 1));
+          ev = (y >= L.h - 2) ? T(0) : DIVW(E(cx, cy) + E(cx, cy + 1), F(cx, cy) + F(cx, cy + 1));
         else
           ev = (x >= L.w - 2 || y >= L.h - 2)
                    ? T(0)
-                   : (((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1)) /
-                         WS(F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1));
+                   : DIVW(((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1),
+                          F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1));
         e[q] = e[q] + ev;
       }
     team_sync(team);
@@ -938,7 +956,10 @@ MgArgs level_args(MgLevel &L, const float *in, float *out, int ns, float alpha) 
   a.alpha = alpha;
   a.ihsq = 1.0f / L.hh / L.hh;
   a.nsweeps = ns;
-  for (int k = 0; k < 5; k++) a.wsum[k] = (float)((double)(float)k + 0.0001);
+  for (int k = 0; k < 5; k++) {
+    a.wsum[k] = (float)((double)(float)k + 0.0001);
+    a.rwsum[k] = 1.0f / a.wsum[k];
+  }
   a.rfac = 1.0f / 16.0f;
   a.tile = -1;
   return a;
@@ -992,7 +1013,10 @@ void run_tail_t(MgHier &mg, int lt, const S *rhs_top, S *e_top, const float *rfa
   a.rhs_pitch = top.pitch;
   a.e_top = e_top;
   a.e_pitch = top.pitch;
-  for (int k = 0; k < 5; k++) a.wsum[k] = (float)((double)(float)k + 0.0001);
+  for (int k = 0; k < 5; k++) {
+    a.wsum[k] = (float)((double)(float)k + 0.0001);
+    a.rwsum[k] = 1.0f / a.wsum[k];
+  }
   size_t smem = fw * sizeof(T) + bw;
   if (smem > TAIL_SMEM_MAX) throw ArgError("coarse levels exceed the tail kernel's shared memory");
   k_mg_tail<S, T><<<1, dim3(32, 32), smem, st>>>(a);
@@ -1221,7 +1245,10 @@ MgArgsT<S> level_args_lo(MgHier &mg, MgLow &lo, int l, int cin, int ns) {
   a.ihsq = 1.0f;
   a.nsweeps = ns;
   a.zero_init = 0;
-  for (int k = 0; k < 5; k++) a.wsum[k] = (float)((double)(float)k + 0.0001);
+  for (int k = 0; k < 5; k++) {
+    a.wsum[k] = (float)((double)(float)k + 0.0001);
+    a.rwsum[k] = 1.0f / a.wsum[k];
+  }
   a.rfac = lo.rfac[l];
   a.tile = -1;
   return a;

@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
                                                  const StepScalars *__restrict__ sc, int comps) {
   const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
   const int W = v.W, H = v.H, P = v.pitch;
-  const float a = sc->a, den = sc->den;
+  const float a = sc->a, den = sc->den, rden = sc->rden;
   if (blockIdx.z == 0) {
     // vx: interior faces x in [1, W-3], y in [1, H-2]
     if (!(comps & 1) || y < 1 || y >= H - 1 || x > W - 3 || x + 3 < 1) return;
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
       val = val + ((k & FC_T2) ? t2 : 0.0f);
       val = val + ((k & FC_T3) ? comp(N, j) : -c);
       val = val + ((k & FC_T4) ? comp(S, j) : -c);
-      o[j] = (k & FC_M) ? (c + a * val) / den : 0.0f;
+      o[j] = (k & FC_M) ? div_rn(c + a * val, den, rden) : 0.0f;
     }
     st4_masked(v.vx[1 - srcx] + (size_t)y * P, x, 1, W - 3, o);
   } else {
@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
       val = val + ((k & FC_T2) ? comp(N, j) : 0.0f);
       val = val + ((k & FC_T3) ? t3 : -c);
       val = val + ((k & FC_T4) ? t4 : -c);
-      o[j] = (k & FC_M) ? (c + a * val) / den : 0.0f;
+      o[j] = (k & FC_M) ? div_rn(c + a * val, den, rden) : 0.0f;
     }
     st4_masked(v.vy[1 - srcy] + (size_t)y * P, x, 1, W - 2, o);
   }
@@ -538,8 +538,16 @@ __global__ void __launch_bounds__(256) k_gradient(VelBufs v, int fx, int fy,
     if (y <= H - 3) st4_masked(vy + (size_t)y * P, x, 1, W - 2, oy);
   }
   if (umax_bits) {
+    // one atomic per block: per-warp atomics on one address serialise
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(umax_bits, __float_as_uint(m));
+    __shared__ float red[VX * VY / 32];
+    const int tid = threadIdx.y * VX + threadIdx.x;
+    if ((tid & 31) == 0) red[tid >> 5] = m;
+    __syncthreads();
+    if (tid == 0) {
+      for (int i = 1; i < VX * VY / 32; i++) m = fmaxf(m, red[i]);
+      atomicMax(umax_bits, __float_as_uint(m));
+    }
   }
 }
 
@@ -573,6 +581,7 @@ __global__ void k_cfl_scalars(const unsigned int *umax_bits, float cfl, float h,
   s.dt = dt;
   s.a = dt * mu * ((float)W - 1.0f) / pwidth;
   s.den = 1.0f + 4.0f * s.a;
+  s.rden = __frcp_rn(s.den);
   s.ih = 1.0f / h;
   s.chalf = 0.5f * dt * s.ih;
   s.cfull = dt * s.ih;

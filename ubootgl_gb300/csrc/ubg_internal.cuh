@@ -55,6 +55,7 @@ struct StepScalars {
   float dt;
   float a;      // dt * mu * (width - 1.0f) / pwidth
   float den;    // 1.0f + 4.0f * a
+  float rden;   // RN(1 / den), for div_rn
   float ih;     // 1.0f / h
   float chalf;  // 0.5f * dt * ih
   float cfull;  // dt * ih
@@ -118,6 +119,26 @@ void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const Ste
 // the previous step's gradient and boundary kernels is used as is.
 void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, float pwidth,
                 unsigned int *umax_bits, StepScalars *sc, cudaStream_t st, bool umax_ready);
+
+// x / d, correctly rounded, for a divisor d > 0 with r = RN(1 / d):
+// Markstein's correction (P. Markstein, "Computation of elementary functions
+// on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990):
+// q0 = RN(x r), the remainder x - q0 d is exact in one FMA, and RN(q0 + rem r)
+// is RN(x / d) when nothing underflows or overflows.  Zeros, tiny, huge and
+// non-finite x take the division itself.
+__device__ __forceinline__ float div_rn(float x, float d, float r) {
+  const float ax = fabsf(x);
+  if (ax >= 0x1p-100f && ax <= 0x1p+100f) {
+    const float q0 = x * r;
+    const float rem = __fmaf_rn(-q0, d, x);
+    return __fmaf_rn(rem, r, q0);
+  }
+  return x / d;
+}
+
+// Compares div_rn(x[i], d, RN(1/d)) with x[i] / d bit for bit on the device
+// (NaNs compare equal); host arrays.
+int selftest_div_rn(const float *x, int n, float d, unsigned *mismatches);
 
 // ------------------------------------------------- game-side field access
 void launch_scatter_accum(float *ax, float *ay, int P, int W, int H, const float2 *xy,
