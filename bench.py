@@ -31,7 +31,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 W_DEFAULT, H_DEFAULT = 4096, 2048
-METRIC = "Mcell-steps/s at 4096x2048 (FP32, reference step: 2 V-cycles)"
+# the headline metric as the benchmark specification names it; `value` is the
+# FP32 drop-in (the reference's step: 2 V-cycles), `modes` the mixed
+# solvers and `served` the p50/p99 latencies
+METRIC = "Mcell-steps/s at 4096x2048 (FP32 vs mixed, \u22641e-5 resid); served p50/p99 latency"
 
 
 def dist_env():
@@ -230,14 +233,9 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     prof = sim.profile_read()
-    ms = ev0.elapsed_time(ev1)
-    if pg:
-        t = torch.tensor([ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_step = ms / args.steps
     cells = W * H
-    value = cells * args.steps * world / (ms / 1e3) / 1e6
+    ms, value = replica_throughput(ev0.elapsed_time(ev1), cells, args.steps, world, pg, dev)
+    ms_step = ms / args.steps
     launches_per_step = prof["kernel_launches"]
 
     # ---- dominant kernel timing (CUDA events on the handle's stream)
@@ -246,6 +244,9 @@ def run_ours(args):
     # ---- end-to-end through the C ABI with host buffers
     e2e = end_to_end(sim, L, lib, W, H, max(3, min(args.steps, args.e2e_steps)), barrier, pg,
                      world, dev)
+
+    if rank != 0:
+        return
 
     # ---- the mixed-precision solver on the same workload (extension)
     modes = {}
@@ -267,8 +268,6 @@ def run_ours(args):
                     L, lib, args.serve_sessions, rate, dur, args.serve_budget_gb,
                     args.serve_active, prec)
 
-    if rank != 0:
-        return
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mcell-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
@@ -276,6 +275,8 @@ def run_ours(args):
         "data": "synthetic (seeded disc mask + smoothed-noise velocity)",
         "config": {"workload": "fluid step %dx%d, 12 discs, FP32, 2 V-cycles, dt=0.5h/max|u| on device"
                                % (W, H),
+                   "solver": "FP32 drop-in: the reference's step with its 2 V-cycles (value); "
+                             "mixed FP16/BF16 solvers in modes; served stream in served",
                    "grid": [W, H], "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2: step working set %.0f MB > 129 MB"
                          % (working_set_bytes(W, H) / 1e6)},
@@ -465,6 +466,19 @@ def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, preci
             "offered_mcell_steps_per_s": round(offered / 1e6, 1),
             "device_gb": round(st["device_bytes_used"] / 2 ** 30, 2), "budget_gb": budget_gb,
             "max_active": max_active, "precision": precision, "wall_s": round(wall, 2)}
+
+
+def replica_throughput(ms_local, cells, steps, world, pg, device):
+    """Replicas only: every rank steps its own grid; the job's time is the
+    slowest rank's (MAX over ranks) and the job's throughput counts every
+    rank's cells.  Returns (ms, Mcell-steps/s)."""
+    ms = float(ms_local)
+    if pg is not None and world > 1:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, cells * steps * world / (ms / 1e3) / 1e6
 
 
 def working_set_bytes(W, H):

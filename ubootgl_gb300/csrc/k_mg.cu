@@ -256,6 +256,7 @@ struct Tile {
 // the tile are still exact, so each half sweep updates just that cone.
 template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float>
 __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg(MgArgsT<S> a) {
+  griddep_wait();
   constexpr int NTY = NT / 32;
   using T = Tile<TX, TY, HALO>;
   using St = Sto<S>;
@@ -599,6 +600,7 @@ __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg
 __global__ void k_residual(const float *__restrict__ p, const float *__restrict__ rhs,
                            const uint8_t *__restrict__ flag, int w, int h, int P, float ihsq,
                            float *r, double *norm2) {
+  griddep_wait();
   int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
   double acc = 0.0;
   if (x < w && y < h) {
@@ -700,6 +702,7 @@ __device__ __forceinline__ void team_sync(int team) {
 // for the FP64 coarse solve of the mixed solver).
 template <class S, class T>
 __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs<S> a) {
+  griddep_wait();
   using St = Sto<S>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *fm = reinterpret_cast<T *>(smem_raw);
@@ -850,7 +853,7 @@ template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float>
 void launch_mg_t(const MgArgsT<S> &a, cudaStream_t st) {
   using T = Tile<TX, TY, HALO>;
   dim3 grid((a.w + TX - 1) / TX, (a.h + TY - 1) / TY);
-  k_mg<TX, TY, HALO, A1, NT, S><<<grid, dim3(32, NT / 32), T::smem(sizeof(S)), st>>>(a);
+  launch_pdl(k_mg<TX, TY, HALO, A1, NT, S>, grid, dim3(32, NT / 32), T::smem(sizeof(S)), st, a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -1019,7 +1022,7 @@ void run_tail_t(MgHier &mg, int lt, const S *rhs_top, S *e_top, const float *rfa
   }
   size_t smem = fw * sizeof(T) + bw;
   if (smem > TAIL_SMEM_MAX) throw ArgError("coarse levels exceed the tail kernel's shared memory");
-  k_mg_tail<S, T><<<1, dim3(32, 32), smem, st>>>(a);
+  launch_pdl(k_mg_tail<S, T>, dim3(1), dim3(32, 32), smem, st, a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -1104,6 +1107,7 @@ struct DcArgs {
 // ||r||^2 (FP32 per warp, FP64 across warps) and max|r|.
 template <class S>
 __global__ void __launch_bounds__(256) k_dc_resid(DcArgs<S> a) {
+  griddep_wait();
   using St = Sto<S>;
   const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
   const int w = a.w, h = a.h;
@@ -1154,6 +1158,7 @@ __global__ void __launch_bounds__(256) k_dc_resid(DcArgs<S> a) {
 template <class S>
 __global__ void __launch_bounds__(256) k_dc_scale(const float *__restrict__ r, S *g, int w, int h,
                                                   int pitch, DcScalars *sc, float h0sq, int kexp) {
+  griddep_wait();
   using St = Sto<S>;
   const float m = __uint_as_float(sc->maxbits) * h0sq;
   float mul = 0.0f, inv = 0.0f;
@@ -1182,6 +1187,7 @@ __global__ void __launch_bounds__(256) k_dc_scale(const float *__restrict__ r, S
 __global__ void __launch_bounds__(256) k_fmean_reduce(const float *__restrict__ f,
                                                       const uint8_t *__restrict__ code, int w,
                                                       int h, int pitch, double *acc) {
+  griddep_wait();
   const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
   float v = 0.0f;
   bool in = false;
@@ -1221,6 +1227,7 @@ __global__ void __launch_bounds__(256) k_fmean_reduce(const float *__restrict__ 
 __global__ void __launch_bounds__(256) k_fmean_apply(float *f, const uint8_t *__restrict__ code,
                                                      int w, int h, int pitch,
                                                      const double *acc) {
+  griddep_wait();
   const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
   if (x < 1 || x >= w - 1 || y < 1 || y >= h - 1) return;
   const double n = acc[2];

@@ -133,6 +133,7 @@ __device__ void vbc_component(const float *s, float *b0, float *b1, int pitch, i
 
 __global__ void k_vbc(VelBufs v, int fx, int fy, Bcs bc, int do_vx, int do_vy,
                       unsigned int *umax_bits) {
+  griddep_wait();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int W = v.W, H = v.H;
   int nx = (H - 2) + (W - 1);
@@ -152,6 +153,7 @@ __global__ void k_vbc(VelBufs v, int fx, int fy, Bcs bc, int do_vx, int do_vy,
 
 // ---------------------------------------------- applyAccumulatedVelocity
 __global__ void k_accum(float *vx, float *vy, float *ax, float *ay, int pitch, int W, int H) {
+  griddep_wait();
   int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
   size_t i = (size_t)y * pitch + x;
   if (x >= 1 && x < W - 2 && y >= 1 && y < H - 1) {
@@ -250,6 +252,7 @@ __device__ __forceinline__ void st4_masked(float *row, int x, int lo, int hi, co
 
 __global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
                                                  const StepScalars *__restrict__ sc, int comps) {
+  griddep_wait();
   const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
   const int W = v.W, H = v.H, P = v.pitch;
   const float a = sc->a, den = sc->den, rden = sc->rden;
@@ -367,6 +370,7 @@ constexpr int AD_SW = AD_TX + 2 * AD_H, AD_SH = AD_TY + 2 * AD_H;
 
 __global__ void __launch_bounds__(256) k_advect(VelBufs v, int srcx, int srcy,
                                                 const StepScalars *__restrict__ sc) {
+  griddep_wait();
   __shared__ float sxv[AD_SH * AD_SW];
   __shared__ float syv[AD_SH * AD_SW];
   __shared__ uint8_t scx[AD_TY * AD_TX], scy[AD_TY * AD_TX];
@@ -454,6 +458,7 @@ __global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ vx
                                                     const float *__restrict__ vy,
                                                     float *__restrict__ f, int P, int W, int H,
                                                     const StepScalars *__restrict__ sc) {
+  griddep_wait();
   const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
   if (y < 1 || y >= H - 1 || x > W - 2 || x + 3 < 1) return;
   const float ih = sc->ih;
@@ -469,6 +474,7 @@ __global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ vx
 }
 
 __global__ void k_sinks(float *f, int P, const SinkCell *cells, int n) {
+  griddep_wait();
   // The reference writes the cells in list order; later sinks win.
   if (blockIdx.x == 0 && threadIdx.x == 0)
     for (int i = 0; i < n; i++) f[(size_t)cells[i].y * P + cells[i].x] = cells[i].v;
@@ -476,6 +482,7 @@ __global__ void k_sinks(float *f, int P, const SinkCell *cells, int n) {
 
 // ------------------------------------------------------------------ setPBC
 __global__ void k_pbc(float *p, int P, int W, int H, Bcs bc) {
+  griddep_wait();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   auto at = [&](int x, int y) -> float & { return p[(size_t)y * P + x]; };
   if (t < H - 2) {
@@ -510,6 +517,7 @@ __global__ void __launch_bounds__(256) k_gradient(VelBufs v, int fx, int fy,
                                                   const float *__restrict__ p,
                                                   const StepScalars *__restrict__ sc,
                                                   unsigned int *umax_bits) {
+  griddep_wait();
   const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
   const int W = v.W, H = v.H, P = v.pitch;
   float m = 0.0f;
@@ -555,6 +563,7 @@ __global__ void __launch_bounds__(256) k_gradient(VelBufs v, int fx, int fy,
 __global__ void __launch_bounds__(256) k_umax(const float *__restrict__ vx,
                                               const float *__restrict__ vy, int P, int W, int H,
                                               unsigned int *umax_bits) {
+  griddep_wait();
   // grid-stride over rows; one atomic per block
   float m = 0.0f;
   for (int y = blockIdx.y * 8 + threadIdx.y; y < H; y += gridDim.y * 8)
@@ -574,6 +583,7 @@ __global__ void __launch_bounds__(256) k_umax(const float *__restrict__ vx,
 
 __global__ void k_cfl_scalars(const unsigned int *umax_bits, float cfl, float h, float mu,
                               float pwidth, int W, StepScalars *sc) {
+  griddep_wait();
   float umax = __uint_as_float(*umax_bits);
   umax = umax > 1e-7f ? umax : 1e-7f;
   float dt = cfl * h / umax;
@@ -605,14 +615,14 @@ void launch_vbc(const VelBufs &v, int fx, int fy, Bcs bc, bool do_vx, bool do_vy
                 unsigned int *umax_bits) {
   ProfScope ps_(KC_VBC, st);
   int n = (v.H - 2) + (v.W - 1) + (v.H - 3) + v.W;
-  k_vbc<<<(n + 255) / 256, 256, 0, st>>>(v, fx, fy, bc, do_vx, do_vy, umax_bits);
+  launch_pdl(k_vbc, dim3((n + 255) / 256), dim3(256), 0, st, v, fx, fy, bc, do_vx, do_vy, umax_bits);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
 
 void launch_accum(const VelBufs &v, int fx, int fy, float *ax, float *ay, cudaStream_t st) {
   ProfScope ps_(KC_ACCUM, st);
-  k_accum<<<grid2(v.W, v.H), dim3(BX, BY), 0, st>>>(v.vx[fx], v.vy[fy], ax, ay, v.pitch, v.W, v.H);
+  launch_pdl(k_accum, grid2(v.W, v.H), dim3(BX, BY), 0, st, v.vx[fx], v.vy[fy], ax, ay, v.pitch, v.W, v.H);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -620,7 +630,7 @@ void launch_accum(const VelBufs &v, int fx, int fy, float *ax, float *ay, cudaSt
 void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, int comps,
                           cudaStream_t st) {
   ProfScope ps_(KC_DIFFUSE, st);
-  k_diffuse<<<grid_vec(v.W, v.H, 2), dim3(VX, VY), 0, st>>>(v, srcx, srcy, sc, comps);
+  launch_pdl(k_diffuse, grid_vec(v.W, v.H, 2), dim3(VX, VY), 0, st, v, srcx, srcy, sc, comps);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -628,7 +638,7 @@ void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const StepScalar
 void launch_advect(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, cudaStream_t st) {
   ProfScope ps_(KC_ADVECT, st);
   dim3 grid((v.W + AD_TX - 1) / AD_TX, (v.H + AD_TY - 1) / AD_TY);
-  k_advect<<<grid, dim3(BX, BY), 0, st>>>(v, srcx, srcy, sc);
+  launch_pdl(k_advect, grid, dim3(BX, BY), 0, st, v, srcx, srcy, sc);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -636,8 +646,8 @@ void launch_advect(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, 
 void launch_divergence(const VelBufs &v, int fx, int fy, float *f, const StepScalars *sc,
                        cudaStream_t st) {
   ProfScope ps_(KC_DIVERGENCE, st);
-  k_divergence<<<grid_vec(v.W, v.H), dim3(VX, VY), 0, st>>>(v.vx[fx], v.vy[fy], f, v.pitch, v.W,
-                                                           v.H, sc);
+  launch_pdl(k_divergence, grid_vec(v.W, v.H), dim3(VX, VY), 0, st, v.vx[fx], v.vy[fy], f,
+             v.pitch, v.W, v.H, sc);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -653,7 +663,7 @@ void launch_sinks(float *f, int pitch, const SinkCell *cells, int n, cudaStream_
 void launch_pbc(float *p, int pitch, int W, int H, Bcs bc, cudaStream_t st) {
   ProfScope ps_(KC_PBC, st);
   int n = (H - 2) + W;
-  k_pbc<<<(n + 255) / 256, 256, 0, st>>>(p, pitch, W, H, bc);
+  launch_pdl(k_pbc, dim3((n + 255) / 256), dim3(256), 0, st, p, pitch, W, H, bc);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -661,7 +671,7 @@ void launch_pbc(float *p, int pitch, int W, int H, Bcs bc, cudaStream_t st) {
 void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const StepScalars *sc,
                      unsigned int *umax_bits, cudaStream_t st) {
   ProfScope ps_(KC_GRADIENT, st);
-  k_gradient<<<grid_vec(v.W, v.H), dim3(VX, VY), 0, st>>>(v, fx, fy, p, sc, umax_bits);
+  launch_pdl(k_gradient, grid_vec(v.W, v.H), dim3(VX, VY), 0, st, v, fx, fy, p, sc, umax_bits);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -670,7 +680,7 @@ void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, 
                 unsigned int *umax_bits, StepScalars *sc, cudaStream_t st, bool umax_ready) {
   ProfScope ps_(KC_CFL, st);
   if (umax_ready) {
-    k_cfl_scalars<<<1, 1, 0, st>>>(umax_bits, cfl, h, mu, pwidth, v.W, sc);
+    launch_pdl(k_cfl_scalars, dim3(1), dim3(1), 0, st, umax_bits, cfl, h, mu, pwidth, v.W, sc);
     UBG_LAUNCH_CHECK();
     g_stats.launches++;
     return;
@@ -678,9 +688,9 @@ void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, 
   UBG_CUDA(cudaMemsetAsync(umax_bits, 0, sizeof(unsigned int), st));
   dim3 g((v.W + BX - 1) / BX, 64);
   if (g.x > 16) g.x = 16;
-  k_umax<<<g, dim3(BX, BY), 0, st>>>(v.vx[fx], v.vy[fy], v.pitch, v.W, v.H, umax_bits);
+  launch_pdl(k_umax, g, dim3(BX, BY), 0, st, v.vx[fx], v.vy[fy], v.pitch, v.W, v.H, umax_bits);
   UBG_LAUNCH_CHECK();
-  k_cfl_scalars<<<1, 1, 0, st>>>(umax_bits, cfl, h, mu, pwidth, v.W, sc);
+  launch_pdl(k_cfl_scalars, dim3(1), dim3(1), 0, st, umax_bits, cfl, h, mu, pwidth, v.W, sc);
   UBG_LAUNCH_CHECK();
   g_stats.launches += 2;
 }

@@ -42,6 +42,28 @@ struct ArgError : std::runtime_error {
 
 #define UBG_LAUNCH_CHECK() UBG_CUDA(cudaGetLastError())
 
+// Programmatic dependent launch: the kernel may be scheduled while its
+// predecessor on the stream drains (the launch latency overlaps the
+// predecessor's last wave); every kernel launched this way starts with
+// griddep_wait(), so no thread reads memory before the predecessor grid has
+// completed and its writes are visible.
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  UBG_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+}
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
 // Sets the message returned by ubg_last_error() on the calling thread.
