@@ -325,14 +325,61 @@ __device__ __forceinline__ float cr_dot(const CrW &w, float A, float B, float C,
   return __fmaf_rn(w.d, D, __fmaf_rn(w.c, C, __fmaf_rn(w.b, B, w.a * A)));
 }
 
-// Catmull-Rom sample from 16 values (rows r0..r3 of a 4x4 stencil).
+// Packed FP32 (two lanes per instruction, sm_100 and later): each lane is
+// the IEEE single-precision operation with round-to-nearest, so every lane
+// equals the scalar operation it replaces.
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+
+// The two weight sets of one sample at once: lane x for t.x, lane y for t.y
+// (the operations of cr_weights, lane by lane).
+struct CrW2 {
+  float2 a, b, c, d;
+};
+__device__ __forceinline__ CrW2 cr_weights2(float2 t) {
+  const float2 t2 = f2_mul(t, t);
+  CrW2 w;
+  w.a = f2_mul(t, f2_fma(t, f2_fma(f2(-0.5f), t, f2(1.0f)), f2(-0.5f)));
+  w.b = f2_fma(t2, f2_fma(f2(1.5f), t, f2(-2.5f)), f2(1.0f));
+  w.c = f2_mul(t, f2_fma(t, f2_fma(f2(-1.5f), t, f2(2.0f)), f2(0.5f)));
+  w.d = f2_mul(t2, f2_fma(f2(0.5f), t, f2(-0.5f)));
+  return w;
+}
+
+// Catmull-Rom sample from 16 values (rows r0..r3 of a 4x4 stencil): the
+// four vertical dots cr_dot(wy, column j) two columns per instruction, then
+// the horizontal dot.
 __device__ __forceinline__ float bicubic16(const float *b, int stride, float sx, float sy) {
-  CrW wy = cr_weights(sy), wx = cr_weights(sx);
-  float col[4];
+  const CrW2 w = cr_weights2(make_float2(sy, sx));
+  const float2 wa = f2(w.a.x), wb = f2(w.b.x), wc = f2(w.c.x), wd = f2(w.d.x);
+  float2 col[2];
 #pragma unroll
-  for (int j = 0; j < 4; j++)
-    col[j] = cr_dot(wy, b[j], b[stride + j], b[2 * stride + j], b[3 * stride + j]);
-  return cr_dot(wx, col[0], col[1], col[2], col[3]);
+  for (int j = 0; j < 2; j++) {
+    const float2 A = make_float2(b[2 * j], b[2 * j + 1]);
+    const float2 B = make_float2(b[stride + 2 * j], b[stride + 2 * j + 1]);
+    const float2 C = make_float2(b[2 * stride + 2 * j], b[2 * stride + 2 * j + 1]);
+    const float2 D = make_float2(b[3 * stride + 2 * j], b[3 * stride + 2 * j + 1]);
+    col[j] = f2_fma(wd, D, f2_fma(wc, C, f2_fma(wb, B, f2_mul(wa, A))));
+  }
+  const CrW wx{w.a.y, w.b.y, w.c.y, w.d.y};
+  return cr_dot(wx, col[0].x, col[0].y, col[1].x, col[1].y);
 }
 
 // A staged window of one staggered component: region [sx0, sx0+SW) x
