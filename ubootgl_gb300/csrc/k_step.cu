@@ -325,28 +325,7 @@ __device__ __forceinline__ float cr_dot(const CrW &w, float A, float B, float C,
   return __fmaf_rn(w.d, D, __fmaf_rn(w.c, C, __fmaf_rn(w.b, B, w.a * A)));
 }
 
-// Packed FP32 (two lanes per instruction, sm_100 and later): each lane is
-// the IEEE single-precision operation with round-to-nearest, so every lane
-// equals the scalar operation it replaces.
-__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
-  float2 d;
-  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
-      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
-      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-      : "=f"(d.x), "=f"(d.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-  return d;
-}
-__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
-  float2 d;
-  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
-      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-      : "=f"(d.x), "=f"(d.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return d;
-}
-__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+
 
 // The two weight sets of one sample at once: lane x for t.x, lane y for t.y
 // (the operations of cr_weights, lane by lane).

@@ -142,6 +142,31 @@ void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const Ste
 void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, float pwidth,
                 unsigned int *umax_bits, StepScalars *sc, cudaStream_t st, bool umax_ready);
 
+// Packed FP32 (two lanes per instruction, sm_100 and later): each lane is
+// the IEEE single-precision operation with round-to-nearest, so every lane
+// equals the scalar operation it replaces.  ptxas may fuse a packed product
+// that feeds a packed addition into one fused multiply-add (observed on
+// sm_103a despite .rn), so these are used only where no product is added.
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+
 // x / d, correctly rounded, for a divisor d > 0 with r = RN(1 / d):
 // Markstein's correction (P. Markstein, "Computation of elementary functions
 // on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990):
