@@ -160,13 +160,10 @@ struct ubg_sim {
   void io_consume() {
     if (!io_staged) return;
     UBG_CUDA(cudaStreamWaitEvent(st, io_in_ready, 0));
-    UBG_CUDA(cudaMemcpy2DAsync(v.vx[fx], (size_t)P * 4, io_in[0], (size_t)P * 4, (size_t)(W - 1) * 4,
-                               H, cudaMemcpyDeviceToDevice, st));
-    UBG_CUDA(cudaMemcpy2DAsync(v.vy[fy], (size_t)P * 4, io_in[1], (size_t)P * 4, (size_t)W * 4, H - 1,
-                               cudaMemcpyDeviceToDevice, st));
+    launch_stage_in(v, fx, fy, io_in[0], io_in[1], d_umax, st);
     UBG_CUDA(cudaEventRecord(io_in_free, st));
     io_staged = false;
-    umax_ready = false;
+    umax_ready = true;  // the copy kernel folded max|u| of the new fields
   }
 
   void *scratch_get(size_t bytes) {
@@ -1662,10 +1659,7 @@ int ubg_io_download_async(ubg_sim *s, float *vx, float *vy) {
     // snapshot the current fields on the simulation's stream (the next step
     // overwrites them), then copy to the host on the I/O stream
     UBG_CUDA(cudaStreamWaitEvent(s->st, s->io_out_done, 0));
-    UBG_CUDA(cudaMemcpy2DAsync(s->io_out[0], (size_t)s->P * 4, s->v.vx[s->fx], (size_t)s->P * 4,
-                               (size_t)(s->W - 1) * 4, s->H, cudaMemcpyDeviceToDevice, s->st));
-    UBG_CUDA(cudaMemcpy2DAsync(s->io_out[1], (size_t)s->P * 4, s->v.vy[s->fy], (size_t)s->P * 4,
-                               (size_t)s->W * 4, s->H - 1, cudaMemcpyDeviceToDevice, s->st));
+    launch_stage_out(s->v, s->fx, s->fy, s->io_out[0], s->io_out[1], s->st);
     UBG_CUDA(cudaEventRecord(s->io_out_copied, s->st));
     UBG_CUDA(cudaStreamWaitEvent(s->io_out_st, s->io_out_copied, 0));
     UBG_CUDA(cudaMemcpy2DAsync(vx, (size_t)(s->W - 1) * 4, s->io_out[0], (size_t)s->P * 4,

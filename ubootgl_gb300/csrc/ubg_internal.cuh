@@ -139,6 +139,11 @@ void launch_gradient(const VelBufs &v, int fx, int fy, const float *p, const Ste
 // max(|vx|, |vy|) over the front buffers -> dt = cfl*h/max (extension) and
 // the derived scalars.  With umax_ready the maximum left in *umax_bits by
 // the previous step's gradient and boundary kernels is used as is.
+// Staged host I/O: staging -> front velocity (+ max|u| into *umax_bits,
+// zeroed first), and front velocity -> staging.
+void launch_stage_in(VelBufs &v, int fx, int fy, const float *inx, const float *iny,
+                     unsigned int *umax_bits, cudaStream_t st);
+void launch_stage_out(const VelBufs &v, int fx, int fy, float *outx, float *outy, cudaStream_t st);
 void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, float pwidth,
                 unsigned int *umax_bits, StepScalars *sc, cudaStream_t st, bool umax_ready);
 
