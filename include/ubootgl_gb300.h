@@ -235,9 +235,12 @@ int ubg_restore(ubg_sim *sim, const void *src);
 int ubg_autotune(ubg_sim *sim, char *report, size_t len);
 
 /* Batch (extension): n independent simulations of any sizes advanced
- * together.  Each batch step is one CUDA graph launch whose parallel
- * branches are the members' fixed-cycle step bodies, so their kernels run
- * concurrently.  dts: n host time steps, or NULL for dt = cfl * h / max|u|
+ * together, one CUDA graph launch per batch step.  When every member is
+ * FP32 with dt from the device and the members average under 1.5 M cells,
+ * the step is fused: each kernel of the step is one launch over all members
+ * (blocks mapped to members through prefix sums, per-member arguments in a
+ * device table), ~40 launches whatever the member count.  Otherwise the
+ * graph's parallel branches are the members' own step bodies.  dts: n host time steps, or NULL for dt = cfl * h / max|u|
  * per member on the device.  Members keep their own fields, options and
  * streams (ordered after the batch step); each member's result is
  * bit-identical to stepping it alone.  Members need UBG_SOLVE_FIXED and no

@@ -105,3 +105,30 @@ def test_batch_rejects_tolerance_members(lib):
         b.step(cfl=0.5)
     b.close()
     s.close()
+
+
+def test_fused_batch_uneven_many(lib):
+    """A fused batch (one launch per kernel over all members) of 24 members
+    with uneven sizes, hence different multigrid depths and coarse tails:
+    every member bit-identical to stepping alone, also after a member is
+    stepped alone between batch steps (the plan follows its indices)."""
+    from ubootgl_gb300.simulation import Batch
+    rng = np.random.default_rng(9)
+    sizes = [(int(w), int(w) // 2) for w in rng.choice([96, 128, 160, 192, 256, 320, 384, 512], 24)]
+    alone = [build(W, H, 200 + i, u_in=0.5 + 0.04 * i) for i, (W, H) in enumerate(sizes)]
+    members = [build(W, H, 200 + i, u_in=0.5 + 0.04 * i) for i, (W, H) in enumerate(sizes)]
+    batch = Batch(members)
+    for it in range(5):
+        if it == 2:
+            alone[3].step_cfl(0.5)
+            members[3].step_cfl(0.5)
+        for s in alone:
+            s.step_cfl(0.5)
+        batch.step(cfl=0.5)
+    batch.sync()
+    for a, b in zip(alone, members):
+        for n in ("vx", "vy", "vx_back", "vy_back", "p"):
+            assert np.array_equal(a.get(n), b.get(n)), (a.width, n)
+    batch.close()
+    for s in alone + members:
+        s.close()

@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <type_traits>
 
 #define ALPHA_IS_ONE(a) ((a) == 1.0f)
@@ -254,9 +255,8 @@ struct Tile {
 // (no bank conflicts).  Red = (x+y) odd; region parity equals global parity
 // because x0 + y0 is even.  After half sweep i only cells within HALO - i of
 // the tile are still exact, so each half sweep updates just that cone.
-template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float>
-__global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg(MgArgsT<S> a) {
-  griddep_wait();
+template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S>
+__device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, const int by) {
   constexpr int NTY = NT / 32;
   using T = Tile<TX, TY, HALO>;
   using St = Sto<S>;
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg
   auto IDX = [](int rx, int ry) { return (((rx + ry) & 1) * RY + ry) * HX + (rx >> 1); };
 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-  const int x0 = blockIdx.x * TX - HALO, y0 = blockIdx.y * TY - HALO;
+  const int x0 = bx * TX - HALO, y0 = by * TY - HALO;
   const int w = a.w, h = a.h, P = a.pitch;
 
   // ---- load p, f, code (float4 / uchar4 per thread; x0 is a multiple of 4).
@@ -346,17 +346,29 @@ __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg
     uint8_t *scf = reinterpret_cast<uint8_t *>(sc + 2 * RY * HX) +
                    ((size_t)CW * CH * sizeof(S) + 15) / 16 * 16;
     const int cxa = x0 >> 1, cya = y0 >> 1;
-    for (int q = tid; q < CW * CH; q += NT) {
+    // all of a thread's loads in flight together, then the stores
+    constexpr int CQ = CW * CH, CIT = (CQ + NT - 1) / NT;
+    float ev[CIT];
+    uint8_t fv[CIT];
+#pragma unroll
+    for (int it = 0; it < CIT; it++) {
+      int q = tid + it * NT;
       int ly = q / CW, lx = q - ly * CW;
       int cx = cxa + lx, cy = cya + ly;
-      float e = 0.0f;
-      uint8_t fc = 0;
-      if (cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
-        e = St::ldg1(a.ec + (size_t)cy * a.cpitch + cx);
-        fc = __ldg(a.codec + (size_t)cy * a.cpitch + cx) & 1u;
+      ev[it] = 0.0f;
+      fv[it] = 0;
+      if (q < CQ && cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
+        ev[it] = St::ldg1(a.ec + (size_t)cy * a.cpitch + cx);
+        fv[it] = __ldg(a.codec + (size_t)cy * a.cpitch + cx) & 1u;
       }
-      sec[q] = St::fromf(e);
-      scf[q] = fc;
+    }
+#pragma unroll
+    for (int it = 0; it < CIT; it++) {
+      int q = tid + it * NT;
+      if (q < CQ) {
+        sec[q] = St::fromf(ev[it]);
+        scf[q] = fv[it];
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -577,7 +589,7 @@ __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg
   }
   // ---- restrict (pressure_solver.cpp:118-132) onto the coarse tile -------
   if (a.rc) {
-    const int cx0 = blockIdx.x * (TX / 2), cy0 = blockIdx.y * (TY / 2);
+    const int cx0 = bx * (TX / 2), cy0 = by * (TY / 2);
     for (int q = tid; q < (TX / 2) * (TY / 2); q += NT) {
       int cyy = q / (TX / 2), cxx = q - cyy * (TX / 2);
       int X = cx0 + cxx, Y = cy0 + cyy;
@@ -594,6 +606,22 @@ __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg
       a.rc[(size_t)Y * a.cpitch + X] = St::fromf(v);
     }
   }
+}
+
+template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float>
+__global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg(MgArgsT<S> a) {
+  griddep_wait();
+  k_mg_body<TX, TY, HALO, ALPHA1, NT, S>(a, blockIdx.x, blockIdx.y);
+}
+// One launch over the members of a batch (FP32): block -> member -> tile.
+template <int TX, int TY, int HALO, bool ALPHA1, int NT>
+__global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4))
+    k_mg_m(const MgArgs *__restrict__ A, const int *__restrict__ bs, int n) {
+  griddep_wait();
+  const int m = member_of(bs, n);
+  const MgArgs &a = A[m];
+  const int l = (int)blockIdx.x - __ldg(bs + m), gx = (a.w + TX - 1) / TX;
+  k_mg_body<TX, TY, HALO, ALPHA1, NT, float>(a, l % gx, l / gx);
 }
 
 // ------------------------------------------------------ residual field only
@@ -701,8 +729,7 @@ __device__ __forceinline__ void team_sync(int team) {
 // the mixed solver); T: arithmetic and shared-memory type (float, or double
 // for the FP64 coarse solve of the mixed solver).
 template <class S, class T>
-__global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs<S> a) {
-  griddep_wait();
+__device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
   using St = Sto<S>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *fm = reinterpret_cast<T *>(smem_raw);
@@ -848,6 +875,17 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs<S> a) {
       a.e_top[(size_t)y * a.e_pitch + x] = St::fromf((float)fm[L0.oe + y * L0.w + x]);
 }
 
+template <class S, class T>
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs<S> a) {
+  griddep_wait();
+  k_mg_tail_body<S, T>(a);
+}
+// One block per member of a batch (FP32).
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail_m(const TailArgs<float> *__restrict__ A) {
+  griddep_wait();
+  k_mg_tail_body<float, float>(A[blockIdx.x]);
+}
+
 // ------------------------------------------------------------ launches
 template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float>
 void launch_mg_t(const MgArgsT<S> &a, cudaStream_t st) {
@@ -886,9 +924,28 @@ void set_vcycle_attrs() {
   set_smem_attr<112, 114, 8, true, 1024, S>();
 }
 
+template <int TX, int TY, int HALO>
+void set_multi_attr() {
+  constexpr int NT = TX == 112 && TY == 50 ? 512 : (TX == 112 && TY == 114 ? 1024 : 256);
+  UBG_CUDA(cudaFuncSetAttribute(k_mg_m<TX, TY, HALO, true, NT>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)Tile<TX, TY, HALO>::smem(4)));
+  UBG_CUDA(cudaFuncSetAttribute(k_mg_m<TX, TY, HALO, true, NT>,
+                                cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+}
+
 void init_kernel_attributes() {
   static bool done = false;
   if (done) return;
+  set_multi_attr<112, 50, 8>();
+  set_multi_attr<48, 16, 8>();
+  set_multi_attr<40, 8, 12>();
+  set_multi_attr<112, 24, 8>();
+  set_multi_attr<48, 40, 8>();
+  set_multi_attr<112, 114, 8>();
+  UBG_CUDA(cudaFuncSetAttribute(k_mg_tail_m, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TAIL_SMEM_MAX));
+  UBG_CUDA(cudaFuncSetAttribute(k_mg_tail_m, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   set_vcycle_attrs<float>();
   set_smem_attr<56, 24, 4, false>();
   set_tail_attr<float, float>();
@@ -983,9 +1040,8 @@ size_t tail_smem_bytes(const std::vector<MgLevel> &lv, int lt, size_t elem_bytes
 // scaled: the h^2-scaled form of the mixed solver (hh = 1, ihsq = 1,
 // restriction weights rfac[level]); else the reference's form.
 template <class S, class T>
-void run_tail_t(MgHier &mg, int lt, const S *rhs_top, S *e_top, const float *rfac,
-                cudaStream_t st) {
-  ProfScope ps_(KC_TAIL, st);
+TailArgs<S> tail_args(MgHier &mg, int lt, const S *rhs_top, S *e_top, const float *rfac,
+                      size_t *smem_out) {
   TailArgs<S> a{};
   int nl = mg.levels - 1 - lt;
   a.nlev = nl;
@@ -1022,6 +1078,16 @@ void run_tail_t(MgHier &mg, int lt, const S *rhs_top, S *e_top, const float *rfa
   }
   size_t smem = fw * sizeof(T) + bw;
   if (smem > TAIL_SMEM_MAX) throw ArgError("coarse levels exceed the tail kernel's shared memory");
+  *smem_out = smem;
+  return a;
+}
+
+template <class S, class T>
+void run_tail_t(MgHier &mg, int lt, const S *rhs_top, S *e_top, const float *rfac,
+                cudaStream_t st) {
+  ProfScope ps_(KC_TAIL, st);
+  size_t smem = 0;
+  TailArgs<S> a = tail_args<S, T>(mg, lt, rhs_top, e_top, rfac, &smem);
   launch_pdl(k_mg_tail<S, T>, dim3(1), dim3(32, 32), smem, st, a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
@@ -1721,6 +1787,122 @@ int mg_solve_mixed(MgHier &mg, MgLow &lo, double tol, int max_cycles, double fno
   if (lo.levels != mg.levels) throw std::runtime_error("mixed-precision hierarchy not allocated");
   if (lo.prec == UBG_MIXED_FP16) return solve_mixed_t<__half>(mg, lo, tol, max_cycles, fnorm2, rel, st);
   return solve_mixed_t<__nv_bfloat16>(mg, lo, tol, max_cycles, fnorm2, rel, st);
+}
+
+// ------------------------------------------------- fused batch V-cycle
+namespace {
+int tile_for(const MgLevel &L, int choice) {
+  if (tile_ok(choice, 3)) return choice;
+  return L.w >= 1200 ? 0 : 1;  // the width rule of launch_mg for 3 sweeps
+}
+int tile_tx(int id) { return id == 0 || id == 3 || id == 5 ? 112 : (id == 2 ? 40 : 48); }
+int tile_ty(int id) {
+  const int ty[kTiles] = {50, 16, 8, 24, 40, 114};
+  return ty[id];
+}
+template <class A>
+void slot_add(MultiSlot &s, const A &a, int blocks) {
+  const char *p = reinterpret_cast<const char *>(&a);
+  s.args.insert(s.args.end(), p, p + sizeof(A));
+  if (s.bs.empty()) s.bs.push_back(0);
+  s.bs.push_back(s.bs.back() + blocks);
+  s.blocks += blocks;
+  s.n++;
+}
+}  // namespace
+
+void mg_multi_vcycle(const std::vector<MgHier *> &mgs, std::vector<MultiSlot> &out) {
+  init_kernel_attributes();
+  const int n = (int)mgs.size();
+  int maxt = 0;
+  for (auto *m : mgs) {
+    if (m->tail_top < 1) throw ArgError("fused batch: a member has no coarse tail");
+    maxt = std::max(maxt, m->tail_top);
+  }
+  // per member and level: which e[] holds the level's current values
+  std::vector<std::vector<int>> cur(n);
+  for (int i = 0; i < n; i++) {
+    cur[i].assign(mgs[i]->levels, 0);
+    cur[i][0] = mgs[i]->cur0;
+  }
+  auto level_slots = [&](int l, bool pre) {
+    std::map<int, MultiSlot> by_tile;
+    for (int i = 0; i < n; i++) {
+      MgHier &mg = *mgs[i];
+      if (l >= mg.tail_top) continue;
+      MgLevel &L = mg.lv[l], &C = mg.lv[l + 1];
+      MgArgs a = level_args(L, L.e[cur[i][l]], L.e[1 - cur[i][l]], 3, 1.0f);
+      a.zgbc = l == 0;
+      if (pre) {
+        a.zero_init = l > 0;
+        a.rc = C.rhs;
+        a.cw = C.w;
+        a.ch = C.h;
+        a.cpitch = C.pitch;
+      } else {
+        a.ec = C.e[cur[i][l + 1]];
+        a.codec = C.code;
+        a.cpitch = C.pitch;
+        a.cw = C.w;
+        a.ch = C.h;
+      }
+      const int id = tile_for(L, pre ? L.tile_pre : L.tile_post);
+      a.tile = id;
+      MultiSlot &sl = by_tile[id];
+      sl.kind = MK_MG;
+      sl.tile = id;
+      const int tx = tile_tx(id), ty = tile_ty(id);
+      slot_add(sl, a, ((L.w + tx - 1) / tx) * ((L.h + ty - 1) / ty));
+      cur[i][l] ^= 1;
+    }
+    for (auto &kv : by_tile) out.push_back(std::move(kv.second));
+  };
+  for (int l = 0; l < maxt; l++) level_slots(l, true);
+  {
+    MultiSlot sl;
+    sl.kind = MK_TAIL;
+    for (int i = 0; i < n; i++) {
+      MgHier &mg = *mgs[i];
+      const int lt = mg.tail_top;
+      size_t smem = 0;
+      TailArgs<float> a = tail_args<float, float>(mg, lt, mg.lv[lt].rhs, mg.lv[lt].e[0], nullptr,
+                                                  &smem);
+      sl.smem = std::max(sl.smem, smem);
+      slot_add(sl, a, 1);
+      cur[i][lt] = 0;
+    }
+    out.push_back(std::move(sl));
+  }
+  for (int l = maxt - 1; l >= 0; l--) level_slots(l, false);
+  for (int i = 0; i < n; i++)
+    if (cur[i][0] != mgs[i]->cur0) throw std::runtime_error("fused V-cycle parity");
+}
+
+void launch_multi_mg(const MultiSlot &slot, const void *dargs, const int *dbs, cudaStream_t st) {
+  if (slot.kind == MK_TAIL) {
+    launch_pdl(k_mg_tail_m, dim3(slot.n), dim3(32, 32), slot.smem, st,
+               (const TailArgs<float> *)dargs);
+  } else {
+    const MgArgs *A = (const MgArgs *)dargs;
+    switch (slot.tile) {
+#define UBG_MULTI_TILE(ID, TX, TY, HALO, NT)                                                   \
+  case ID:                                                                                     \
+    launch_pdl(k_mg_m<TX, TY, HALO, true, NT>, dim3(slot.blocks), dim3(32, NT / 32),          \
+               Tile<TX, TY, HALO>::smem(4), st, A, dbs, slot.n);                               \
+    break;
+      UBG_MULTI_TILE(0, 112, 50, 8, 512)
+      UBG_MULTI_TILE(1, 48, 16, 8, 256)
+      UBG_MULTI_TILE(2, 40, 8, 12, 256)
+      UBG_MULTI_TILE(3, 112, 24, 8, 256)
+      UBG_MULTI_TILE(4, 48, 40, 8, 256)
+      UBG_MULTI_TILE(5, 112, 114, 8, 1024)
+#undef UBG_MULTI_TILE
+      default:
+        throw ArgError("fused batch: smoother tile id");
+    }
+  }
+  UBG_LAUNCH_CHECK();
+  g_stats.launches++;
 }
 
 void mg_set_h(MgHier &mg, float h0) {

@@ -131,10 +131,9 @@ __device__ void vbc_component(const float *s, float *b0, float *b1, int pitch, i
   }
 }
 
-__global__ void k_vbc(VelBufs v, int fx, int fy, Bcs bc, int do_vx, int do_vy,
-                      unsigned int *umax_bits) {
-  griddep_wait();
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_vbc_body(VelBufs v, int fx, int fy, Bcs bc, int do_vx, int do_vy,
+                      unsigned int *umax_bits, const int bx, const int by, const int bz) {
+  int t = bx * blockDim.x + threadIdx.x;
   int W = v.W, H = v.H;
   int nx = (H - 2) + (W - 1);
   float m = 0.0f;
@@ -149,6 +148,11 @@ __global__ void k_vbc(VelBufs v, int fx, int fy, Bcs bc, int do_vx, int do_vy,
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(umax_bits, __float_as_uint(m));
   }
+}
+__global__ void k_vbc(VelBufs v, int fx, int fy, Bcs bc, int do_vx, int do_vy,
+                      unsigned int *umax_bits) {
+  griddep_wait();
+  k_vbc_body(v, fx, fy, bc, do_vx, do_vy, umax_bits, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ---------------------------------------------- applyAccumulatedVelocity
@@ -250,13 +254,12 @@ __device__ __forceinline__ void st4_masked(float *row, int x, int lo, int hi, co
   }
 }
 
-__global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
-                                                 const StepScalars *__restrict__ sc, int comps) {
-  griddep_wait();
-  const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
+__device__ __forceinline__ void k_diffuse_body(VelBufs v, int srcx, int srcy,
+                                                 const StepScalars *__restrict__ sc, int comps, const int bx, const int by, const int bz) {
+  const int x = 4 * (bx * VX + threadIdx.x), y = by * VY + threadIdx.y;
   const int W = v.W, H = v.H, P = v.pitch;
   const float a = sc->a, den = sc->den, rden = sc->rden;
-  if (blockIdx.z == 0) {
+  if (bz == 0) {
     // vx: interior faces x in [1, W-3], y in [1, H-2]
     if (!(comps & 1) || y < 1 || y >= H - 1 || x > W - 3 || x + 3 < 1) return;
     const float *s = v.vx[srcx];
@@ -301,6 +304,11 @@ __global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
     }
     st4_masked(v.vy[1 - srcy] + (size_t)y * P, x, 1, W - 2, o);
   }
+}
+__global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
+                                                 const StepScalars *__restrict__ sc, int comps) {
+  griddep_wait();
+  k_diffuse_body(v, srcx, srcy, sc, comps, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ----------------------------------------------------------------- advect
@@ -394,16 +402,15 @@ __device__ __forceinline__ float bicubic_win(const Win &wn, const float *__restr
 constexpr int AD_TX = 64, AD_TY = 16, AD_H = 4;
 constexpr int AD_SW = AD_TX + 2 * AD_H, AD_SH = AD_TY + 2 * AD_H;
 
-__global__ void __launch_bounds__(256) k_advect(VelBufs v, int srcx, int srcy,
-                                                const StepScalars *__restrict__ sc) {
-  griddep_wait();
+__device__ __forceinline__ void k_advect_body(VelBufs v, int srcx, int srcy,
+                                                const StepScalars *__restrict__ sc, const int bx, const int by, const int bz) {
   __shared__ float sxv[AD_SH * AD_SW];
   __shared__ float syv[AD_SH * AD_SW];
   __shared__ uint8_t scx[AD_TY * AD_TX], scy[AD_TY * AD_TX];
   const int W = v.W, H = v.H, P = v.pitch;
   const float *vx = v.vx[srcx];
   const float *vy = v.vy[srcy];
-  const int X0 = blockIdx.x * AD_TX, Y0 = blockIdx.y * AD_TY;
+  const int X0 = bx * AD_TX, Y0 = by * AD_TY;
   const int sx0 = X0 - AD_H, sy0 = Y0 - AD_H;
   const int tid = threadIdx.y * BX + threadIdx.x;
   for (int i = tid; i < AD_SH * AD_SW; i += 256) {
@@ -478,14 +485,18 @@ __global__ void __launch_bounds__(256) k_advect(VelBufs v, int srcx, int srcy,
     }
   }
 }
+__global__ void __launch_bounds__(256) k_advect(VelBufs v, int srcx, int srcy,
+                                                const StepScalars *__restrict__ sc) {
+  griddep_wait();
+  k_advect_body(v, srcx, srcy, sc, blockIdx.x, blockIdx.y, blockIdx.z);
+}
 
 // ------------------------------------------------------------- divergence
-__global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ vx,
+__device__ __forceinline__ void k_divergence_body(const float *__restrict__ vx,
                                                     const float *__restrict__ vy,
                                                     float *__restrict__ f, int P, int W, int H,
-                                                    const StepScalars *__restrict__ sc) {
-  griddep_wait();
-  const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
+                                                    const StepScalars *__restrict__ sc, const int bx, const int by, const int bz) {
+  const int x = 4 * (bx * VX + threadIdx.x), y = by * VY + threadIdx.y;
   if (y < 1 || y >= H - 1 || x > W - 2 || x + 3 < 1) return;
   const float ih = sc->ih;
   float4 U = ld4(vx, P, x, y), V = ld4(vy, P, x, y), Vs = ld4(vy, P, x, y - 1);
@@ -498,6 +509,13 @@ __global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ vx
   }
   st4_masked(f + (size_t)y * P, x, 1, W - 2, o);
 }
+__global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ vx,
+                                                    const float *__restrict__ vy,
+                                                    float *__restrict__ f, int P, int W, int H,
+                                                    const StepScalars *__restrict__ sc) {
+  griddep_wait();
+  k_divergence_body(vx, vy, f, P, W, H, sc, blockIdx.x, blockIdx.y, blockIdx.z);
+}
 
 __global__ void k_sinks(float *f, int P, const SinkCell *cells, int n) {
   griddep_wait();
@@ -507,9 +525,8 @@ __global__ void k_sinks(float *f, int P, const SinkCell *cells, int n) {
 }
 
 // ------------------------------------------------------------------ setPBC
-__global__ void k_pbc(float *p, int P, int W, int H, Bcs bc) {
-  griddep_wait();
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_pbc_body(float *p, int P, int W, int H, Bcs bc, const int bx, const int by, const int bz) {
+  int t = bx * blockDim.x + threadIdx.x;
   auto at = [&](int x, int y) -> float & { return p[(size_t)y * P + x]; };
   if (t < H - 2) {
     int y = t + 1;
@@ -535,16 +552,19 @@ __global__ void k_pbc(float *p, int P, int W, int H, Bcs bc) {
   at(x, 0) = single_pbc(bc.s, a1);
   at(x, H - 1) = single_pbc(bc.n, a2);
 }
+__global__ void k_pbc(float *p, int P, int W, int H, Bcs bc) {
+  griddep_wait();
+  k_pbc_body(p, P, W, H, bc, blockIdx.x, blockIdx.y, blockIdx.z);
+}
 
 // ---------------------------------------------------------------- gradient
 // Pressure-gradient update; also folds max(|vx|, |vy|) of every interior
 // face (after the update) into *umax_bits for the next step's CFL dt.
-__global__ void __launch_bounds__(256) k_gradient(VelBufs v, int fx, int fy,
+__device__ __forceinline__ void k_gradient_body(VelBufs v, int fx, int fy,
                                                   const float *__restrict__ p,
                                                   const StepScalars *__restrict__ sc,
-                                                  unsigned int *umax_bits) {
-  griddep_wait();
-  const int x = 4 * (blockIdx.x * VX + threadIdx.x), y = blockIdx.y * VY + threadIdx.y;
+                                                  unsigned int *umax_bits, const int bx, const int by, const int bz) {
+  const int x = 4 * (bx * VX + threadIdx.x), y = by * VY + threadIdx.y;
   const int W = v.W, H = v.H, P = v.pitch;
   float m = 0.0f;
   if (y >= 1 && y < H - 1 && x <= W - 2 && x + 3 >= 1) {
@@ -583,6 +603,13 @@ __global__ void __launch_bounds__(256) k_gradient(VelBufs v, int fx, int fy,
       atomicMax(umax_bits, __float_as_uint(m));
     }
   }
+}
+__global__ void __launch_bounds__(256) k_gradient(VelBufs v, int fx, int fy,
+                                                  const float *__restrict__ p,
+                                                  const StepScalars *__restrict__ sc,
+                                                  unsigned int *umax_bits) {
+  griddep_wait();
+  k_gradient_body(v, fx, fy, p, sc, umax_bits, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ------------------------------------------------------ staged host I/O
@@ -659,9 +686,8 @@ __global__ void __launch_bounds__(256) k_umax(const float *__restrict__ vx,
   }
 }
 
-__global__ void k_cfl_scalars(const unsigned int *umax_bits, float cfl, float h, float mu,
-                              float pwidth, int W, StepScalars *sc) {
-  griddep_wait();
+__device__ __forceinline__ void k_cfl_scalars_body(const unsigned int *umax_bits, float cfl, float h, float mu,
+                              float pwidth, int W, StepScalars *sc, const int bx, const int by, const int bz) {
   float umax = __uint_as_float(*umax_bits);
   umax = umax > 1e-7f ? umax : 1e-7f;
   float dt = cfl * h / umax;
@@ -675,12 +701,72 @@ __global__ void k_cfl_scalars(const unsigned int *umax_bits, float cfl, float h,
   s.cfull = dt * s.ih;
   *sc = s;
 }
+__global__ void k_cfl_scalars(const unsigned int *umax_bits, float cfl, float h, float mu,
+                              float pwidth, int W, StepScalars *sc) {
+  griddep_wait();
+  k_cfl_scalars_body(umax_bits, cfl, h, mu, pwidth, W, sc, blockIdx.x, blockIdx.y, blockIdx.z);
+}
 
 inline dim3 grid2(int w, int h, int z = 1) { return dim3((w + BX - 1) / BX, (h + BY - 1) / BY, z); }
 inline dim3 grid_vec(int w, int h, int z = 1) {
   return dim3((w + 4 * VX - 1) / (4 * VX), (h + VY - 1) / VY, z);
 }
 
+
+// ---------------------------------------------------- multi-member kernels
+__global__ void k_vbc_m(const VbcM *__restrict__ A, const int *__restrict__ bs, int n) {
+  griddep_wait();
+  const int m = member_of(bs, n);
+  const VbcM a = A[m];
+  k_vbc_body(a.v, a.fx, a.fy, a.bc, a.do_vx, a.do_vy, a.umax, (int)blockIdx.x - __ldg(bs + m), 0, 0);
+}
+__global__ void __launch_bounds__(256) k_diffuse_m(const DiffuseM *__restrict__ A,
+                                                   const int *__restrict__ bs, int n) {
+  griddep_wait();
+  const int m = member_of(bs, n);
+  const DiffuseM a = A[m];
+  const int l = (int)blockIdx.x - __ldg(bs + m);
+  k_diffuse_body(a.v, a.srcx, a.srcy, a.sc, a.comps, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
+}
+__global__ void __launch_bounds__(256) k_advect_m(const AdvectM *__restrict__ A,
+                                                  const int *__restrict__ bs, int n) {
+  griddep_wait();
+  const int m = member_of(bs, n);
+  const AdvectM a = A[m];
+  const int l = (int)blockIdx.x - __ldg(bs + m);
+  k_advect_body(a.v, a.srcx, a.srcy, a.sc, l % a.gx, l / a.gx, 0);
+}
+__global__ void __launch_bounds__(256) k_divergence_m(const DivergenceM *__restrict__ A,
+                                                      const int *__restrict__ bs, int n) {
+  griddep_wait();
+  const int m = member_of(bs, n);
+  const DivergenceM a = A[m];
+  const int l = (int)blockIdx.x - __ldg(bs + m);
+  k_divergence_body(a.vx, a.vy, a.f, a.P, a.W, a.H, a.sc, l % a.gx, l / a.gx, 0);
+}
+__global__ void k_pbc_m(const PbcM *__restrict__ A, const int *__restrict__ bs, int n) {
+  griddep_wait();
+  const int m = member_of(bs, n);
+  const PbcM a = A[m];
+  const int l = (int)blockIdx.x - __ldg(bs + m);
+  if (l == 0 && threadIdx.x == 0 && a.umax_zero) *a.umax_zero = 0u;
+  k_pbc_body(a.p, a.P, a.W, a.H, a.bc, l, 0, 0);
+}
+__global__ void __launch_bounds__(256) k_gradient_m(const GradientM *__restrict__ A,
+                                                    const int *__restrict__ bs, int n) {
+  griddep_wait();
+  const int m = member_of(bs, n);
+  const GradientM a = A[m];
+  const int l = (int)blockIdx.x - __ldg(bs + m);
+  k_gradient_body(a.v, a.fx, a.fy, a.p, a.sc, a.umax, l % a.gx, l / a.gx, 0);
+}
+__global__ void k_cfl_m(const CflM *__restrict__ A, int n) {
+  griddep_wait();
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const CflM a = A[m];
+  k_cfl_scalars_body(a.umax, a.cfl, a.h, a.mu, a.pwidth, a.W, a.sc, 0, 0, 0);
+}
 }  // namespace
 
 void launch_face_codes(const VelBufs &v, const uint8_t *flag, uint8_t *cx, uint8_t *cy,
@@ -791,4 +877,64 @@ void launch_cfl(const VelBufs &v, int fx, int fy, float cfl, float h, float mu, 
   g_stats.launches += 2;
 }
 
+}  // namespace ubg
+
+namespace ubg {
+int multi_blocks_vbc(const VbcM &a) {
+  int n = (a.v.H - 2) + (a.v.W - 1) + (a.v.H - 3) + a.v.W;
+  return (n + 255) / 256;
+}
+int multi_blocks_diffuse(DiffuseM &a) {
+  dim3 g = grid_vec(a.v.W, a.v.H, 2);
+  a.gx = (int)g.x;
+  a.gy = (int)g.y;
+  return (int)(g.x * g.y * g.z);
+}
+int multi_blocks_advect(AdvectM &a) {
+  a.gx = (a.v.W + AD_TX - 1) / AD_TX;
+  return a.gx * ((a.v.H + AD_TY - 1) / AD_TY);
+}
+int multi_blocks_divergence(DivergenceM &a) {
+  dim3 g = grid_vec(a.W, a.H);
+  a.gx = (int)g.x;
+  return (int)(g.x * g.y);
+}
+int multi_blocks_pbc(const PbcM &a) { return ((a.H - 2) + a.W + 255) / 256; }
+int multi_blocks_gradient(GradientM &a) {
+  dim3 g = grid_vec(a.v.W, a.v.H);
+  a.gx = (int)g.x;
+  return (int)(g.x * g.y);
+}
+
+void launch_multi_step(int kind, const void *args, const int *bs, int n, int blocks,
+                       cudaStream_t st) {
+  switch (kind) {
+    case MK_VBC:
+      launch_pdl(k_vbc_m, dim3(blocks), dim3(256), 0, st, (const VbcM *)args, bs, n);
+      break;
+    case MK_DIFFUSE:
+      launch_pdl(k_diffuse_m, dim3(blocks), dim3(VX, VY), 0, st, (const DiffuseM *)args, bs, n);
+      break;
+    case MK_ADVECT:
+      launch_pdl(k_advect_m, dim3(blocks), dim3(BX, BY), 0, st, (const AdvectM *)args, bs, n);
+      break;
+    case MK_DIVERGENCE:
+      launch_pdl(k_divergence_m, dim3(blocks), dim3(VX, VY), 0, st, (const DivergenceM *)args, bs,
+                 n);
+      break;
+    case MK_PBC:
+      launch_pdl(k_pbc_m, dim3(blocks), dim3(256), 0, st, (const PbcM *)args, bs, n);
+      break;
+    case MK_GRADIENT:
+      launch_pdl(k_gradient_m, dim3(blocks), dim3(VX, VY), 0, st, (const GradientM *)args, bs, n);
+      break;
+    case MK_CFL:
+      launch_pdl(k_cfl_m, dim3((n + 127) / 128), dim3(128), 0, st, (const CflM *)args, n);
+      break;
+    default:
+      throw ArgError("multi-member launch kind");
+  }
+  UBG_LAUNCH_CHECK();
+  g_stats.launches++;
+}
 }  // namespace ubg

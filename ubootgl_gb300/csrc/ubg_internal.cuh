@@ -203,6 +203,90 @@ void launch_set_grids(const int2 *cells, const uint8_t *val, const uint8_t *zero
 void launch_shift_map(VelBufs &v, int fx, int fy, const float *p_in, float *p_out,
                       const uint8_t *flag, int P, int W, int H, float inlet_u, cudaStream_t st);
 
+// ------------------------------------- multi-member (fused batch) launches
+// One launch covers every member of a batch: the grid is the concatenation
+// of the members' grids, bs[m] the first block of member m (bs[n] = total),
+// and each block runs the single-simulation kernel body on its member's
+// arguments.  Arguments live in a device table built by the host.
+enum MultiKind {
+  MK_VBC = 0, MK_DIFFUSE, MK_ADVECT, MK_DIVERGENCE, MK_PBC, MK_GRADIENT, MK_CFL, MK_MG, MK_TAIL
+};
+struct VbcM {
+  VelBufs v;
+  int fx, fy, do_vx, do_vy;
+  Bcs bc;
+  unsigned int *umax;
+};
+struct DiffuseM {
+  VelBufs v;
+  int srcx, srcy, comps, gx, gy;
+  const StepScalars *sc;
+};
+struct AdvectM {
+  VelBufs v;
+  int srcx, srcy, gx;
+  const StepScalars *sc;
+};
+struct DivergenceM {
+  const float *vx, *vy;
+  float *f;
+  int P, W, H, gx;
+  const StepScalars *sc;
+};
+struct PbcM {
+  float *p;
+  int P, W, H;
+  Bcs bc;
+  unsigned int *umax_zero;  // zeroed by the member's first thread (next: gradient)
+};
+struct GradientM {
+  VelBufs v;
+  int fx, fy, gx;
+  const float *p;
+  const StepScalars *sc;
+  unsigned int *umax;
+};
+struct CflM {
+  const unsigned int *umax;
+  float cfl, h, mu, pwidth;
+  int W;
+  StepScalars *sc;
+};
+// The member of the block in a multi-member launch: the largest m with
+// bs[m] <= blockIdx.x.
+__device__ __forceinline__ int member_of(const int *__restrict__ bs, int n) {
+  const int b = (int)blockIdx.x;
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(bs + mid) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One launch of a fused batch step: `n` members, their argument structs
+// back to back, the block prefix sums and the dynamic shared memory.
+struct MultiSlot {
+  int kind = 0;
+  int tile = -1;  // MK_MG: smoother tile id
+  int n = 0;
+  int blocks = 0;
+  size_t smem = 0;
+  std::vector<char> args;
+  std::vector<int> bs;
+};
+// Blocks a member needs for each kind (and fills the grid width fields).
+int multi_blocks_vbc(const VbcM &a);
+int multi_blocks_diffuse(DiffuseM &a);
+int multi_blocks_advect(AdvectM &a);
+int multi_blocks_divergence(DivergenceM &a);
+int multi_blocks_pbc(const PbcM &a);
+int multi_blocks_gradient(GradientM &a);
+// Launches over n members (device tables args, bs; total blocks).
+void launch_multi_step(int kind, const void *args, const int *bs, int n, int blocks,
+                       cudaStream_t st);
+
 // ------------------------------------------------------------ multigrid
 struct MgLevel {
   int w, h, pitch;
@@ -233,6 +317,15 @@ struct MgHier {
 // buffers) and keeps the fastest; results are bit-identical for every
 // choice.  Appends a JSON report to *report if given.
 void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report);
+
+// The launches of one V-cycle (MG::solve with zero-gradient edges, FP32) of
+// every member, fused level by level: pre-smoothing launches from level 0
+// down, one tail launch (each member's one-CTA coarse solve), then the
+// post-smoothing launches back up.  Members of a level are grouped by their
+// smoother tile.  Every member needs a coarse tail (tail_top >= 1).
+void mg_multi_vcycle(const std::vector<MgHier *> &mgs, std::vector<MultiSlot> &out);
+// Launches one MK_MG / MK_TAIL slot whose tables are at dargs / dbs.
+void launch_multi_mg(const MultiSlot &slot, const void *dargs, const int *dbs, cudaStream_t st);
 
 // Allocates the hierarchy for a W x H level-0 grid with spacing h0.
 void mg_alloc(MgHier &mg, int W, int H, float h0);
