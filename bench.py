@@ -262,11 +262,12 @@ def run_ours(args):
             batched[prec] = batch_bench(L, lib, args.batch, args.batch_steps, args.warmup, prec)
     if args.serve_sessions > 0:
         for prec in args.serve_precisions.split(","):
-            for rate, dur in ((args.serve_rate, args.serve_seconds),
-                              (args.serve_rate_low, args.serve_seconds)):
-                served["%s_%g_per_s" % (prec, rate)] = serve_bench(
-                    L, lib, args.serve_sessions, rate, dur, args.serve_budget_gb,
-                    args.serve_active, prec)
+            for mode in args.serve_modes.split(","):
+                for rate, dur in ((args.serve_rate, args.serve_seconds),
+                                  (args.serve_rate_low, args.serve_seconds)):
+                    served["%s_%s_%g_per_s" % (prec, mode, rate)] = serve_bench(
+                        L, lib, args.serve_sessions, rate, dur, args.serve_budget_gb,
+                        args.serve_active, prec, mode)
 
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mcell-steps/s", "n_gpus": world,
@@ -401,20 +402,23 @@ def batch_bench(L, lib, n, steps, warmup, precision, seed=11):
             "widths": "log-uniform [128, 2048], h = w/2", "timing": "host wall clock, synchronised"}
 
 
-def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, precision, seed=5):
+def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, precision, mode,
+                seed=5, wmin=256, wmax=4096, fuse_cells=None):
     """Served stream: step requests arrive as a Poisson process (`rate` per
     second for `duration` seconds) over n_sessions resident sessions with
-    widths log-uniform in [256, 4096] (height = width / 2), each asking for
+    widths log-uniform in [wmin, wmax] (height = width / 2), each asking for
     k ~ U[1, 20] device-CFL steps; sessions admitted under a device-memory
     budget.  Session fields are crops of one seeded 4096 x 2048 instance
-    (walls re-applied, own inflow speed)."""
+    (walls re-applied, own inflow speed).  mode: the server's stepping mode
+    ("fused" continuous batching or per-session "streams")."""
     from ubootgl_gb300 import workload as WL
     from ubootgl_gb300.simulation import Server
     rng = np.random.default_rng(seed)
     base_flag, base_vx, base_vy = WL.instance(4096, 2048, seed)
-    srv = Server(int(budget_gb * (1 << 30)), max_active=max_active)
+    srv = Server(int(budget_gb * (1 << 30)), max_active=max_active, mode=mode,
+                 fuse_cells=fuse_cells)
     ids, cells = [], {}
-    for W in WL.log_uniform_widths(n_sessions, 256, 4096, seed + 1):
+    for W in WL.log_uniform_widths(n_sessions, wmin, wmax, seed + 1):
         H = W // 2
         flag = base_flag[:H, :W].copy()
         flag[0, :] = 0.0
@@ -465,7 +469,14 @@ def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, preci
             "value": round(cs / wall / 1e6, 2), "unit": "Mcell-steps/s",
             "offered_mcell_steps_per_s": round(offered / 1e6, 1),
             "device_gb": round(st["device_bytes_used"] / 2 ** 30, 2), "budget_gb": budget_gb,
-            "max_active": max_active, "precision": precision, "wall_s": round(wall, 2)}
+            "fused_steps": st["fused_steps"] - srv2_base["fused_steps"],
+            "fused_member_steps": st["fused_member_steps"] - srv2_base["fused_member_steps"],
+            "worker_ms": {"fused": round(st["worker_fused_ms"] - srv2_base["worker_fused_ms"], 1),
+                          "streams": round(st["worker_streams_ms"]
+                                           - srv2_base["worker_streams_ms"], 1)},
+            "widths": [wmin, wmax], "max_active": max_active, "precision": precision,
+            "mode": mode,
+            "wall_s": round(wall, 2)}
 
 
 def replica_throughput(ms_local, cells, steps, world, pg, device):
@@ -635,6 +646,7 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-active", type=int, default=32)
     ap.add_argument("--serve-precisions", default="fp32")
+    ap.add_argument("--serve-modes", default="fused,streams")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

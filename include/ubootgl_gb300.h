@@ -271,11 +271,16 @@ int ubg_selftest_div(const float *x, int n, float d, unsigned *mismatches);
  * against a device-memory budget when opened (UBG_EBUSY and a rejection
  * count when the budget is exhausted).  A request asks for `steps` device-CFL
  * steps of one session.  A worker thread admits queued requests in arrival
- * order while fewer than max_active are in flight (one per session),
- * enqueues each admitted request's steps on its session's stream and
- * retires requests as their streams complete, so requests arriving while
- * others run join as slots free up and the device overlaps all in-flight
- * sessions.  Latency = completion - submission. */
+ * order, one in flight per session, while fewer than max_active stream
+ * requests (or 4 * max_active fused requests) are in flight.  In
+ * the fused mode (the default) the worker enqueues one step of every
+ * in-flight request of an FP32 fixed-mode session of at most 2^20 cells
+ * (ubg_server_set_fuse_cells) per iteration, as one launch per kernel over
+ * all of them, on a high-priority stream: a request joins at the next step
+ * boundary and leaves after its last step.  Other sessions, and every
+ * session in the stream mode, enqueue all their steps on their own stream
+ * and the device overlaps the streams.  Either way a session's results are
+ * bit-identical to stepping it alone.  Latency = completion - submission. */
 typedef struct ubg_server ubg_server;
 typedef struct ubg_serve_stats {
   int sessions, queued, active;
@@ -283,9 +288,20 @@ typedef struct ubg_serve_stats {
   size_t device_bytes_used;
   double busy_ms;              /* first admission to last completion */
   double p50_ms, p99_ms, max_ms; /* request latencies so far */
+  long long fused_steps;         /* fused launch sequences enqueued */
+  long long fused_member_steps;  /* session steps they covered */
+  double worker_fused_ms;        /* worker time spent enqueueing fused steps */
+  double worker_streams_ms;      /* worker time spent enqueueing stream requests */
 } ubg_serve_stats;
 int ubg_server_create(size_t budget_bytes, int max_active, ubg_server **out);
 int ubg_server_destroy(ubg_server *srv);
+#define UBG_SERVE_STREAMS 0 /* every request on its session's stream */
+#define UBG_SERVE_FUSED 1   /* fused steps over the in-flight requests (default) */
+/* Selects how later-admitted requests are stepped. */
+int ubg_server_set_mode(ubg_server *srv, int mode);
+/* The largest session (in cells) the fused mode steps fused (default 2^20);
+ * larger sessions take their own stream. */
+int ubg_server_set_fuse_cells(ubg_server *srv, long long max_cells);
 /* Opens a session (Simulation(flag, pwidth, mu); vx / vy may be NULL, else
  * they initialise both buffers; opt may be NULL). */
 int ubg_server_open(ubg_server *srv, const float *flag, int width, int height, float pwidth,

@@ -1,9 +1,11 @@
 """The step server: results independent of the mix, admission by budget,
 latency statistics.
 
-Each session's kernels touch only that session's memory and run the
-single-simulation path, so a session stepped among many others must be
-bit-identical (tolerance 0) to the same session stepped alone.
+Each session's kernels touch only that session's memory.  In the stream
+mode they run the single-simulation path; in the fused mode one launch per
+kernel covers every in-flight request, and the fused kernels run the same
+per-member arithmetic.  Either way a session stepped among many others must
+be bit-identical (tolerance 0) to the same session stepped alone.
 """
 import numpy as np
 import pytest
@@ -19,13 +21,14 @@ def session_inputs(W, H, seed, u_in=1.0):
     return flag, vx, vy
 
 
-def test_alone_vs_mixed_bit_identical(lib):
+@pytest.mark.parametrize("mode", ["fused", "streams"])
+def test_alone_vs_mixed_bit_identical(lib, mode):
     from ubootgl_gb300.simulation import Server
     sizes = [(256, 128), (512, 256), (128, 64), (384, 192), (1024, 512), (192, 96)]
     rng = np.random.default_rng(0)
     # alone: one session, its requests one after another
     target = (300, 150, 41)
-    solo = Server(8 << 30, max_active=4)
+    solo = Server(8 << 30, max_active=4, mode=mode)
     sid = solo.open(*session_inputs(*target))
     reqs = [3, 1, 5, 2]
     for k in reqs:
@@ -33,7 +36,7 @@ def test_alone_vs_mixed_bit_identical(lib):
     alone = {n: solo.get(sid, n) for n in ("vx", "vy", "p")}
     solo.close()
     # in a mix: the same session among others, requests interleaved
-    mix = Server(8 << 30, max_active=4)
+    mix = Server(8 << 30, max_active=4, mode=mode)
     others = [mix.open(*session_inputs(W, H, 50 + i, 0.6 + 0.15 * i))
               for i, (W, H) in enumerate(sizes)]
     sid = mix.open(*session_inputs(*target))
@@ -85,4 +88,39 @@ def test_mixed_precision_sessions(lib):
     va, vb = srv.get(a, "vx"), srv.get(b, "vx")
     assert np.isfinite(srv.get(a, "p")).all()
     assert np.abs(va - vb).max() <= 0.05 * np.abs(vb).max()
+    srv.close()
+
+
+def test_fused_many_sessions_match_plain_steps(lib):
+    """24 sessions of uneven sizes, requests of 1..8 steps submitted in a
+    burst (requests join and leave the fused step at different step
+    boundaries): every session ends bit-identical to a plain simulation
+    stepped the same number of times."""
+    from ubootgl_gb300.simulation import Server, Simulation
+    rng = np.random.default_rng(4)
+    sizes = [(int(w), int(w) // 2) for w in rng.choice([96, 128, 192, 256, 320, 512, 768], 24)]
+    srv = Server(16 << 30, max_active=24, mode="fused")
+    sids, total = [], []
+    for i, (W, H) in enumerate(sizes):
+        sids.append(srv.open(*session_inputs(W, H, 300 + i, 0.5 + 0.05 * i)))
+        total.append(0)
+    pending = []
+    for rnd in range(3):
+        for j in rng.permutation(len(sids)):
+            k = int(rng.integers(1, 9))
+            pending.append(srv.submit(sids[j], k))
+            total[j] += k
+    for r in pending:
+        srv.wait(r)
+    assert srv.stats()["completed"] == len(pending)
+    for i, (W, H) in enumerate(sizes):
+        flag, vx, vy = session_inputs(W, H, 300 + i, 0.5 + 0.05 * i)
+        sim = Simulation(flag, 1.0, 1e-4)
+        for n, a in (("vx", vx), ("vy", vy), ("vx_back", vx), ("vy_back", vy)):
+            sim.set(n, a)
+        for _ in range(total[i]):
+            sim.step_cfl(0.5)
+        for n in ("vx", "vy", "p"):
+            assert np.array_equal(srv.get(sids[i], n), sim.get(n)), (W, n)
+        sim.close()
     srv.close()

@@ -34,7 +34,9 @@ class ServeStats(C.Structure):
                 ("completed", C.c_longlong), ("rejected_sessions", C.c_longlong),
                 ("cell_steps", C.c_longlong), ("device_bytes_used", C.c_size_t),
                 ("busy_ms", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
-                ("max_ms", C.c_double)]
+                ("max_ms", C.c_double), ("fused_steps", C.c_longlong),
+                ("fused_member_steps", C.c_longlong), ("worker_fused_ms", C.c_double),
+                ("worker_streams_ms", C.c_double)]
 
 
 # name -> (restype, argtypes); every int-returning call is checked
@@ -75,6 +77,8 @@ _SIGS = {
     "ubg_sim_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
     "ubg_server_create": (C.c_int, [C.c_size_t, C.c_int, C.POINTER(_P)]),
     "ubg_server_destroy": (C.c_int, [_P]),
+    "ubg_server_set_mode": (C.c_int, [_P, C.c_int]),
+    "ubg_server_set_fuse_cells": (C.c_int, [_P, C.c_longlong]),
     "ubg_server_open": (C.c_int, [_P, _FP, C.c_int, C.c_int, C.c_float, C.c_float, _FP, _FP,
                                   C.POINTER(Options), C.POINTER(C.c_int)]),
     "ubg_server_close": (C.c_int, [_P, C.c_int]),

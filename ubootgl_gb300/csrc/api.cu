@@ -12,6 +12,7 @@
 #include <unordered_map>
 #include <vector>
 #include <algorithm>
+#include <atomic>
 
 #include "ubg_internal.cuh"
 
@@ -116,8 +117,17 @@ struct ubg_sim {
   int last_vcycles = 0;
   double last_rel = -1.0;  // ||r|| / ||f|| after the last tolerance-mode solve
   // CUDA graph of the fixed-cycle step body
-  cudaGraphExec_t graph = nullptr;
-  int graph_key = -1;
+  // captured step bodies: a step flips the velocity buffers, so steps
+  // alternate between two index states and two graphs
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    int key = -1;
+    long gen = -1;
+    long launches = 0;
+    int fx = 0, fy = 0, cur0 = 0;  // indices after the body
+  };
+  StepGraph graphs[2];
+  int graph_next = 0;
   long gen = 0;  // bumped whenever something baked into a captured step changes
   // profiling
   bool prof = false;
@@ -192,7 +202,8 @@ struct ubg_sim {
 
   ~ubg_sim() {
     if (st) cudaStreamSynchronize(st);
-    if (graph) cudaGraphExecDestroy(graph);
+    for (auto &g : graphs)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto &e : ring_ev)
       if (e) cudaEventDestroy(e);
     for (auto &e : ev_step)
@@ -383,11 +394,16 @@ struct ubg_sim {
     if (graphable) {
       // The body only depends on (fx, fy, cur0) parity and the cycle count.
       int key = (fx << 2) | (fy << 1) | mg.cur0 | (opt.vcycles << 3) | (opt.precision << 24);
-      if (!graph || graph_key != key) capture(key);
-      UBG_CUDA(cudaGraphLaunch(graph, st));
+      StepGraph *g = nullptr;
+      for (auto &c : graphs)
+        if (c.exec && c.key == key && c.gen == gen) g = &c;
+      if (!g) g = &capture(key);
+      UBG_CUDA(cudaGraphLaunch(g->exec, st));
       // replay the index bookkeeping of the captured body
-      advance_indices();
-      g_stats.launches += graph_launches;
+      fx = g->fx;
+      fy = g->fy;
+      mg.cur0 = g->cur0;
+      g_stats.launches += g->launches;
     } else {
       step_body(nsc);
     }
@@ -405,13 +421,15 @@ struct ubg_sim {
     launches_last = g_stats.launches - l0;
   }
 
-  long graph_launches = 0;
-  int after_fx = 0, after_fy = 0, after_cur0 = 0;
-
-  void capture(int key) {
-    if (graph) {
-      cudaGraphExecDestroy(graph);
-      graph = nullptr;
+  // Captures the step body for the current indices into the older of the
+  // two graph slots (an executable graph still in flight is freed by the
+  // driver when it completes).
+  StepGraph &capture(int key) {
+    StepGraph &sg = graphs[graph_next];
+    graph_next ^= 1;
+    if (sg.exec) {
+      cudaGraphExecDestroy(sg.exec);
+      sg.exec = nullptr;
     }
     int fx0 = fx, fy0 = fy, c0 = mg.cur0;
     long l0 = g_stats.launches;
@@ -425,23 +443,19 @@ struct ubg_sim {
       throw;
     }
     UBG_CUDA(cudaStreamEndCapture(st, &g));
-    UBG_CUDA(cudaGraphInstantiate(&graph, g, 0));
+    UBG_CUDA(cudaGraphInstantiate(&sg.exec, g, 0));
     cudaGraphDestroy(g);
-    graph_launches = g_stats.launches - l0;
+    sg.launches = g_stats.launches - l0;
     g_stats.launches = l0;
-    after_fx = fx;
-    after_fy = fy;
-    after_cur0 = mg.cur0;
+    sg.fx = fx;
+    sg.fy = fy;
+    sg.cur0 = mg.cur0;
     fx = fx0;
     fy = fy0;
     mg.cur0 = c0;
-    graph_key = key;
-  }
-
-  void advance_indices() {
-    fx = after_fx;
-    fy = after_fy;
-    mg.cur0 = after_cur0;
+    sg.key = key;
+    sg.gen = gen;
+    return sg;
   }
 
   void sync() { UBG_CUDA(cudaStreamSynchronize(st)); }
@@ -631,7 +645,6 @@ int ubg_set_options(ubg_sim *s, const ubg_options *o) {
     else if (s->lo.prec != o->precision || s->lo.levels != s->mg.levels)
       mg_low_alloc(s->lo, s->mg, o->precision);
     s->opt = *o;
-    s->graph_key = -1;
     s->gen++;
     return UBG_OK;
   });
@@ -643,8 +656,7 @@ int ubg_set_bcs(ubg_sim *s, int west, int east, int north, int south) {
     for (int b : {west, east, north, south})
       if (b < 0 || b > 3) throw ArgError("boundary type");
     s->bc = Bcs{west, east, north, south};
-    s->graph_key = -1;  // boundary types are baked into the captured step
-    s->gen++;
+    s->gen++;  // boundary types are baked into the captured step
     return UBG_OK;
   });
 }
@@ -1395,7 +1407,6 @@ int ubg_restore(ubg_sim *s, const void *src) {
     s->bc = Bcs{hd.bc[0], hd.bc[1], hd.bc[2], hd.bc[3]};
     s->last_dt = hd.last_dt;
     s->accum_dirty = true;
-    s->graph_key = -1;
     s->gen++;
     s->flag_changed();
     s->sync();
@@ -1410,8 +1421,7 @@ int ubg_autotune(ubg_sim *s, char *report, size_t len) {
     s->sync();
     std::string rep;
     mg_autotune(s->mg, s->st, &rep);
-    s->graph_key = -1;  // the captured step uses the old tiles
-    s->gen++;
+    s->gen++;  // the captured step uses the old tiles
     if (report && len) {
       size_t n = std::min(len - 1, rep.size());
       std::memcpy(report, rep.data(), n);
@@ -1420,6 +1430,293 @@ int ubg_autotune(ubg_sim *s, char *report, size_t len) {
     return UBG_OK;
   });
 }
+
+// ------------------------------------------------------- fused stepping
+// Records the launches of one step of every member as fused slots, in the
+// order of ubg_sim::step_body, for the members' current indices; cfl[i] is
+// member i's dt factor.  afx / afy receive the indices after the step.
+void fused_plan(const std::vector<ubg_sim *> &sims, const float *cfl,
+                std::vector<MultiSlot> &slots, std::vector<int> &afx, std::vector<int> &afy) {
+  const int n = (int)sims.size();
+  std::vector<int> fx(n), fy(n);
+  for (int i = 0; i < n; i++) {
+    fx[i] = sims[i]->fx;
+    fy[i] = sims[i]->fy;
+  }
+  auto add = [&](MultiSlot &sl, const void *a, size_t bytes, int blocks) {
+    const char *p = (const char *)a;
+    sl.args.insert(sl.args.end(), p, p + bytes);
+    if (sl.bs.empty()) sl.bs.push_back(0);
+    sl.bs.push_back(sl.bs.back() + blocks);
+    sl.blocks += blocks;
+    sl.n++;
+  };
+  auto vbc = [&](bool dvx, bool dvy, bool umax) {
+    MultiSlot sl;
+    sl.kind = MK_VBC;
+    for (int i = 0; i < n; i++) {
+      ubg_sim *s = sims[i];
+      VbcM a{s->v, fx[i], fy[i], dvx, dvy, s->bc, umax ? s->d_umax : nullptr};
+      add(sl, &a, sizeof(a), multi_blocks_vbc(a));
+    }
+    slots.push_back(std::move(sl));
+  };
+  {  // dt = cfl h / max|u| from the previous step's max|u|
+    MultiSlot sl;
+    sl.kind = MK_CFL;
+    for (int i = 0; i < n; i++) {
+      ubg_sim *s = sims[i];
+      CflM a{s->d_umax, cfl[i], s->h, s->mu, s->pwidth, s->W, s->d_sc};
+      add(sl, &a, sizeof(a), 0);
+    }
+    slots.push_back(std::move(sl));
+  }
+  // diffuse (simulation.cpp:104-162)
+  vbc(false, true, false);
+  for (int k = 0; k < 2; k++) {
+    MultiSlot sl;
+    sl.kind = MK_DIFFUSE;
+    for (int i = 0; i < n; i++) {
+      ubg_sim *s = sims[i];
+      DiffuseM a{s->v, fx[i], fy[i], 3, 0, 0, s->d_sc};
+      int b = multi_blocks_diffuse(a);
+      add(sl, &a, sizeof(a), b);
+      fx[i] ^= 1;
+      fy[i] ^= 1;
+    }
+    slots.push_back(std::move(sl));
+    vbc(true, true, false);
+  }
+  {  // advect
+    MultiSlot sl;
+    sl.kind = MK_ADVECT;
+    for (int i = 0; i < n; i++) {
+      ubg_sim *s = sims[i];
+      AdvectM a{s->v, fx[i], fy[i], 0, s->d_sc};
+      int b = multi_blocks_advect(a);
+      add(sl, &a, sizeof(a), b);
+      fx[i] ^= 1;
+      fy[i] ^= 1;
+    }
+    slots.push_back(std::move(sl));
+  }
+  vbc(true, true, false);
+  {  // project: divergence
+    MultiSlot sl;
+    sl.kind = MK_DIVERGENCE;
+    for (int i = 0; i < n; i++) {
+      ubg_sim *s = sims[i];
+      DivergenceM a{s->v.vx[fx[i]], s->v.vy[fy[i]], s->f(), s->P, s->W, s->H, 0, s->d_sc};
+      int b = multi_blocks_divergence(a);
+      add(sl, &a, sizeof(a), b);
+    }
+    slots.push_back(std::move(sl));
+  }
+  std::vector<MgHier *> mgs;
+  for (auto *s : sims) mgs.push_back(&s->mg);
+  const int vc = sims[0]->opt.vcycles;
+  for (auto *s : sims)
+    if (s->opt.vcycles != vc) throw ArgError("fused batch: members need the same V-cycle count");
+  for (int c = 0; c < vc; c++) mg_multi_vcycle(mgs, slots);
+  {  // setPBC, then the gradient update with max|u| (umax zeroed first)
+    MultiSlot sl;
+    sl.kind = MK_PBC;
+    for (int i = 0; i < n; i++) {
+      ubg_sim *s = sims[i];
+      PbcM a{s->p(), s->P, s->W, s->H, s->bc, s->d_umax};
+      add(sl, &a, sizeof(a), multi_blocks_pbc(a));
+    }
+    slots.push_back(std::move(sl));
+  }
+  {
+    MultiSlot sl;
+    sl.kind = MK_GRADIENT;
+    for (int i = 0; i < n; i++) {
+      ubg_sim *s = sims[i];
+      GradientM a{s->v, fx[i], fy[i], 0, s->p(), s->d_sc, s->d_umax};
+      int b = multi_blocks_gradient(a);
+      add(sl, &a, sizeof(a), b);
+    }
+    slots.push_back(std::move(sl));
+  }
+  vbc(true, true, true);
+  afx = fx;
+  afy = fy;
+}
+
+
+// Packs the slots into one table: arguments and block prefix sums of each
+// slot, 256-byte aligned, each prefix-sum array followed by `tag` (the word
+// the kernels check); returns the bytes.
+size_t fused_pack(const std::vector<MultiSlot> &slots, unsigned tag, std::vector<char> &host,
+                  std::vector<size_t> &aoff, std::vector<size_t> &boff) {
+  aoff.assign(slots.size(), 0);
+  boff.assign(slots.size(), 0);
+  size_t bytes = 0;
+  auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+  for (size_t i = 0; i < slots.size(); i++) {
+    aoff[i] = bytes;
+    bytes += al(slots[i].args.size());
+    boff[i] = bytes;
+    bytes += al((slots[i].bs.size() + 1) * sizeof(int));
+  }
+  host.assign(bytes, 0);
+  for (size_t i = 0; i < slots.size(); i++) {
+    const MultiSlot &sl = slots[i];
+    if (sl.bs.size() != (size_t)sl.n + 1) throw std::logic_error("fused slot prefix sums");
+    std::memcpy(host.data() + aoff[i], sl.args.data(), sl.args.size());
+    std::memcpy(host.data() + boff[i], sl.bs.data(), sl.bs.size() * sizeof(int));
+    std::memcpy(host.data() + boff[i] + sl.bs.size() * sizeof(int), &tag, sizeof(tag));
+  }
+  return bytes;
+}
+
+// A fresh tag for each packed table.
+unsigned fused_tag() {
+  static std::atomic<unsigned> next{0x5eed0001u};
+  return next.fetch_add(2u);
+}
+
+// A word in mapped pinned host memory that the fused kernels flag errors in.
+unsigned *alloc_err_word() {
+  void *p = nullptr;
+  if (cudaHostAlloc(&p, 64, cudaHostAllocMapped) != cudaSuccess) {
+    cudaGetLastError();
+    throw std::bad_alloc();
+  }
+  *(volatile unsigned *)p = 0u;
+  return (unsigned *)p;
+}
+
+void fused_launch(const std::vector<MultiSlot> &slots, const char *dtable,
+                  const std::vector<size_t> &aoff, const std::vector<size_t> &boff, unsigned tag,
+                  unsigned *err, cudaStream_t st) {
+  for (size_t i = 0; i < slots.size(); i++) {
+    const MultiSlot &sl = slots[i];
+    const int *bs = (const int *)(dtable + boff[i]);
+    if (sl.kind == MK_MG || sl.kind == MK_TAIL)
+      launch_multi_mg(sl, dtable + aoff[i], bs, tag, err, st);
+    else
+      launch_multi_step(sl.kind, dtable + aoff[i], bs, sl.n, sl.blocks, tag, err, st);
+  }
+}
+
+namespace ubg {
+struct FusedStepper::Impl {
+  static constexpr int kSlots = 2;  // steps in flight
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[kSlots] = {}, join_ev = nullptr;
+  unsigned *err = nullptr;  // mapped host word
+  bool used[kSlots] = {};
+  char *host[kSlots] = {};
+  void *dev[kSlots] = {};
+  size_t cap[kSlots] = {};
+  int next = 0;
+  std::vector<MultiSlot> slots;
+  std::vector<char> pack;
+  std::vector<size_t> aoff, boff;
+  std::vector<int> afx, afy;
+};
+
+FusedStepper::FusedStepper() : p_(new Impl()) {
+  try {
+    // high priority: a fused step is many short dependent launches, which
+    // would otherwise queue behind the long kernels of other streams
+    int lo = 0, hi = 0;
+    UBG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    UBG_CUDA(cudaStreamCreateWithPriority(&p_->st, cudaStreamNonBlocking, hi));
+    UBG_CUDA(cudaEventCreateWithFlags(&p_->join_ev, cudaEventDisableTiming));
+    for (auto &e : p_->ev) UBG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    p_->err = alloc_err_word();
+  } catch (...) {
+    this->~FusedStepper();
+    throw;
+  }
+}
+
+FusedStepper::~FusedStepper() {
+  if (!p_) return;
+  if (p_->st) cudaStreamSynchronize(p_->st);
+  for (int k = 0; k < Impl::kSlots; k++) {
+    if (p_->host[k]) cudaFreeHost(p_->host[k]);
+    if (p_->dev[k]) cudaFree(p_->dev[k]);
+    if (p_->ev[k]) cudaEventDestroy(p_->ev[k]);
+  }
+  if (p_->join_ev) cudaEventDestroy(p_->join_ev);
+  if (p_->err) cudaFreeHost(p_->err);
+  if (p_->st) cudaStreamDestroy(p_->st);
+  delete p_;
+  p_ = nullptr;
+}
+
+bool FusedStepper::eligible(const ubg_sim *s) {
+  return s->opt.precision == UBG_FP32 && s->opt.solver_mode == UBG_SOLVE_FIXED &&
+         s->opt.vcycles >= 1 && s->mg.tail_top >= 1 && s->sinks.empty() && !s->prof;
+}
+
+int FusedStepper::group(const ubg_sim *s) { return s->opt.vcycles; }
+
+void FusedStepper::join(ubg_sim *s) {
+  s->io_consume();
+  bool accum = s->accum_dirty;
+  if (accum) s->apply_accum();
+  if (!s->umax_ready || accum)
+    launch_cfl(s->v, s->fx, s->fy, 0.5f, s->h, s->mu, s->pwidth, s->d_umax, s->d_sc, s->st, false);
+  s->umax_ready = true;
+  UBG_CUDA(cudaEventRecord(p_->join_ev, s->st));
+  UBG_CUDA(cudaStreamWaitEvent(p_->st, p_->join_ev, 0));
+}
+
+bool FusedStepper::ready() const {
+  return !p_->used[p_->next] || cudaEventQuery(p_->ev[p_->next]) != cudaErrorNotReady;
+}
+
+void FusedStepper::step(const std::vector<ubg_sim *> &sims, const std::vector<float> &cfl) {
+  if (sims.empty()) return;
+  if (cfl.size() != sims.size()) throw ArgError("one cfl per member");
+  Impl &m = *p_;
+  const int k = m.next;
+  m.next = (m.next + 1) % Impl::kSlots;
+  if (m.used[k]) UBG_CUDA(cudaEventSynchronize(m.ev[k]));
+  m.slots.clear();
+  fused_plan(sims, cfl.data(), m.slots, m.afx, m.afy);
+  const unsigned tag = fused_tag();
+  size_t bytes = fused_pack(m.slots, tag, m.pack, m.aoff, m.boff);
+  if (bytes > m.cap[k]) {
+    if (m.host[k]) cudaFreeHost(m.host[k]);
+    if (m.dev[k]) cudaFree(m.dev[k]);
+    m.host[k] = nullptr;
+    m.dev[k] = nullptr;
+    m.cap[k] = 0;
+    size_t b = std::max(bytes * 2, (size_t)1 << 16);
+    if (cudaMallocHost((void **)&m.host[k], b) != cudaSuccess ||
+        cudaMalloc(&m.dev[k], b) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    m.cap[k] = b;
+  }
+  std::memcpy(m.host[k], m.pack.data(), bytes);
+  UBG_CUDA(cudaMemcpyAsync(m.dev[k], m.host[k], bytes, cudaMemcpyHostToDevice, m.st));
+  fused_launch(m.slots, (const char *)m.dev[k], m.aoff, m.boff, tag, m.err, m.st);
+  UBG_CUDA(cudaEventRecord(m.ev[k], m.st));
+  m.used[k] = true;
+  for (size_t i = 0; i < sims.size(); i++) {
+    ubg_sim *s = sims[i];
+    s->fx = m.afx[i];
+    s->fy = m.afy[i];
+    s->umax_ready = true;
+    s->last_vcycles = s->opt.vcycles;
+  }
+}
+
+bool FusedStepper::failed() const { return *(volatile unsigned *)p_->err != 0u; }
+
+void FusedStepper::leave(ubg_sim *s, cudaEvent_t ev) {
+  UBG_CUDA(cudaEventRecord(ev, p_->st));
+  UBG_CUDA(cudaStreamWaitEvent(s->st, ev, 0));
+}
+}  // namespace ubg
 
 // ----------------------------------------------------------------- batch
 // Many independent simulations advanced by one graph launch: each member's
@@ -1431,10 +1728,16 @@ struct ubg_batch {
   cudaStream_t st = nullptr;
   cudaEvent_t fork = nullptr, done = nullptr;
   std::vector<cudaEvent_t> pre, join;
-  cudaGraphExec_t graph = nullptr;
-  std::vector<long long> key;
-  std::vector<int> after_fx, after_fy, after_cur0;
-  long graph_launches = 0;
+  // branch form: one graph per index state (steps alternate between two)
+  struct Branch {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<long long> key;
+    float cfl = -1.0f;
+    std::vector<int> after_fx, after_fy, after_cur0;
+    long launches = 0;
+  };
+  Branch br[2];
+  int br_next = 0;
   // fused form: every launch covers all members (one graph per index parity)
   struct Fused {
     std::vector<long long> key;
@@ -1446,6 +1749,12 @@ struct ubg_batch {
   Fused fused[2];
   int fused_next = 0;
   bool use_fused = true;
+  unsigned *err = nullptr;  // mapped host word the fused kernels flag errors in
+
+  void check_fused() const {
+    if (err && *(volatile unsigned *)err)
+      throw CudaError("fused batch step: a launch found a table it was not made for");
+  }
 
   ~ubg_batch() {
     if (st) cudaStreamSynchronize(st);
@@ -1453,11 +1762,13 @@ struct ubg_batch {
       if (f.exec) cudaGraphExecDestroy(f.exec);
       if (f.table) cudaFree(f.table);
     }
-    if (graph) cudaGraphExecDestroy(graph);
+    for (auto &b : br)
+      if (b.exec) cudaGraphExecDestroy(b.exec);
     for (auto e : pre) cudaEventDestroy(e);
     for (auto e : join) cudaEventDestroy(e);
     if (fork) cudaEventDestroy(fork);
     if (done) cudaEventDestroy(done);
+    if (err) cudaFreeHost(err);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -1472,16 +1783,18 @@ struct ubg_batch {
     return k;
   }
 
-  void capture(bool device_dt, float cfl) {
-    if (graph) {
-      cudaGraphExecDestroy(graph);
-      graph = nullptr;
+  Branch &capture(bool device_dt, float cfl) {
+    Branch &b = br[br_next];
+    br_next ^= 1;
+    if (b.exec) {
+      cudaGraphExecDestroy(b.exec);
+      b.exec = nullptr;
     }
     long l0 = g_stats.launches;
     size_t n = sims.size();
-    after_fx.assign(n, 0);
-    after_fy.assign(n, 0);
-    after_cur0.assign(n, 0);
+    b.after_fx.assign(n, 0);
+    b.after_fy.assign(n, 0);
+    b.after_cur0.assign(n, 0);
     std::vector<int> fx0(n), fy0(n), c00(n);
     for (size_t i = 0; i < n; i++) {
       fx0[i] = sims[i]->fx;
@@ -1501,9 +1814,9 @@ struct ubg_batch {
         s->step_body(0);
         UBG_CUDA(cudaEventRecord(join[i], s->st));
         UBG_CUDA(cudaStreamWaitEvent(st, join[i], 0));
-        after_fx[i] = s->fx;
-        after_fy[i] = s->fy;
-        after_cur0[i] = s->mg.cur0;
+        b.after_fx[i] = s->fx;
+        b.after_fy[i] = s->fy;
+        b.after_cur0[i] = s->mg.cur0;
         s->fx = fx0[i];
         s->fy = fy0[i];
         s->mg.cur0 = c00[i];
@@ -1519,10 +1832,13 @@ struct ubg_batch {
       throw;
     }
     UBG_CUDA(cudaStreamEndCapture(st, &g));
-    UBG_CUDA(cudaGraphInstantiate(&graph, g, 0));
+    UBG_CUDA(cudaGraphInstantiate(&b.exec, g, 0));
     cudaGraphDestroy(g);
-    graph_launches = g_stats.launches - l0;
+    b.launches = g_stats.launches - l0;
     g_stats.launches = l0;
+    b.key = make_key(device_dt);
+    b.cfl = cfl;
+    return b;
   }
 
   // The fused form needs FP32 members in fixed mode with a coarse tail and
@@ -1538,117 +1854,6 @@ struct ubg_batch {
       cells += (double)s->W * s->H;
     }
     return cells / (double)sims.size() < 1.5e6;
-  }
-
-  // Records the launches of one step of every member as fused slots, in
-  // the order of ubg_sim::step_body, for the members' current indices.
-  void plan(float cfl, std::vector<MultiSlot> &slots, std::vector<int> &afx,
-            std::vector<int> &afy) {
-    const int n = (int)sims.size();
-    std::vector<int> fx(n), fy(n);
-    for (int i = 0; i < n; i++) {
-      fx[i] = sims[i]->fx;
-      fy[i] = sims[i]->fy;
-    }
-    auto add = [&](MultiSlot &sl, const void *a, size_t bytes, int blocks) {
-      const char *p = (const char *)a;
-      sl.args.insert(sl.args.end(), p, p + bytes);
-      if (sl.bs.empty()) sl.bs.push_back(0);
-      sl.bs.push_back(sl.bs.back() + blocks);
-      sl.blocks += blocks;
-      sl.n++;
-    };
-    auto vbc = [&](bool dvx, bool dvy, bool umax) {
-      MultiSlot sl;
-      sl.kind = MK_VBC;
-      for (int i = 0; i < n; i++) {
-        ubg_sim *s = sims[i];
-        VbcM a{s->v, fx[i], fy[i], dvx, dvy, s->bc, umax ? s->d_umax : nullptr};
-        add(sl, &a, sizeof(a), multi_blocks_vbc(a));
-      }
-      slots.push_back(std::move(sl));
-    };
-    {  // dt = cfl h / max|u| from the previous step's max|u|
-      MultiSlot sl;
-      sl.kind = MK_CFL;
-      for (int i = 0; i < n; i++) {
-        ubg_sim *s = sims[i];
-        CflM a{s->d_umax, cfl, s->h, s->mu, s->pwidth, s->W, s->d_sc};
-        add(sl, &a, sizeof(a), 0);
-      }
-      slots.push_back(std::move(sl));
-    }
-    // diffuse (simulation.cpp:104-162)
-    vbc(false, true, false);
-    for (int k = 0; k < 2; k++) {
-      MultiSlot sl;
-      sl.kind = MK_DIFFUSE;
-      for (int i = 0; i < n; i++) {
-        ubg_sim *s = sims[i];
-        DiffuseM a{s->v, fx[i], fy[i], 3, 0, 0, s->d_sc};
-        int b = multi_blocks_diffuse(a);
-        add(sl, &a, sizeof(a), b);
-        fx[i] ^= 1;
-        fy[i] ^= 1;
-      }
-      slots.push_back(std::move(sl));
-      vbc(true, true, false);
-    }
-    {  // advect
-      MultiSlot sl;
-      sl.kind = MK_ADVECT;
-      for (int i = 0; i < n; i++) {
-        ubg_sim *s = sims[i];
-        AdvectM a{s->v, fx[i], fy[i], 0, s->d_sc};
-        int b = multi_blocks_advect(a);
-        add(sl, &a, sizeof(a), b);
-        fx[i] ^= 1;
-        fy[i] ^= 1;
-      }
-      slots.push_back(std::move(sl));
-    }
-    vbc(true, true, false);
-    {  // project: divergence
-      MultiSlot sl;
-      sl.kind = MK_DIVERGENCE;
-      for (int i = 0; i < n; i++) {
-        ubg_sim *s = sims[i];
-        DivergenceM a{s->v.vx[fx[i]], s->v.vy[fy[i]], s->f(), s->P, s->W, s->H, 0, s->d_sc};
-        int b = multi_blocks_divergence(a);
-        add(sl, &a, sizeof(a), b);
-      }
-      slots.push_back(std::move(sl));
-    }
-    std::vector<MgHier *> mgs;
-    for (auto *s : sims) mgs.push_back(&s->mg);
-    const int vc = sims[0]->opt.vcycles;
-    for (auto *s : sims)
-      if (s->opt.vcycles != vc) throw ArgError("fused batch: members need the same V-cycle count");
-    for (int c = 0; c < vc; c++) mg_multi_vcycle(mgs, slots);
-    {  // setPBC, then the gradient update with max|u| (umax zeroed first)
-      MultiSlot sl;
-      sl.kind = MK_PBC;
-      for (int i = 0; i < n; i++) {
-        ubg_sim *s = sims[i];
-        PbcM a{s->p(), s->P, s->W, s->H, s->bc, s->d_umax};
-        add(sl, &a, sizeof(a), multi_blocks_pbc(a));
-      }
-      slots.push_back(std::move(sl));
-    }
-    {
-      MultiSlot sl;
-      sl.kind = MK_GRADIENT;
-      for (int i = 0; i < n; i++) {
-        ubg_sim *s = sims[i];
-        GradientM a{s->v, fx[i], fy[i], 0, s->p(), s->d_sc, s->d_umax};
-        int b = multi_blocks_gradient(a);
-        add(sl, &a, sizeof(a), b);
-      }
-      slots.push_back(std::move(sl));
-    }
-    vbc(true, true, true);
-    afx = fx;
-    afy = fy;
   }
 
   Fused &fused_graph(float cfl) {
@@ -1668,40 +1873,26 @@ struct ubg_batch {
       f.table = nullptr;
     }
     std::vector<MultiSlot> slots;
-    plan(cfl, slots, f.after_fx, f.after_fy);
-    // one device table: each slot's arguments and block prefix sums
-    std::vector<size_t> aoff(slots.size()), boff(slots.size());
-    size_t bytes = 0;
-    auto al = [](size_t v) { return (v + 255) / 256 * 256; };
-    for (size_t i = 0; i < slots.size(); i++) {
-      aoff[i] = bytes;
-      bytes += al(slots[i].args.size());
-      boff[i] = bytes;
-      bytes += al(slots[i].bs.size() * sizeof(int));
-    }
-    std::vector<char> host(bytes, 0);
-    for (size_t i = 0; i < slots.size(); i++) {
-      std::memcpy(host.data() + aoff[i], slots[i].args.data(), slots[i].args.size());
-      std::memcpy(host.data() + boff[i], slots[i].bs.data(), slots[i].bs.size() * sizeof(int));
-    }
+    std::vector<float> cfls(sims.size(), cfl);
+    fused_plan(sims, cfls.data(), slots, f.after_fx, f.after_fy);
+    std::vector<char> host;
+    std::vector<size_t> aoff, boff;
+    const unsigned tag = fused_tag();
+    size_t bytes = fused_pack(slots, tag, host, aoff, boff);
     if (cudaMalloc(&f.table, bytes) != cudaSuccess) {
       cudaGetLastError();
       f.table = nullptr;
       throw std::bad_alloc();
     }
-    UBG_CUDA(cudaMemcpy(f.table, host.data(), bytes, cudaMemcpyHostToDevice));
-    char *d = (char *)f.table;
+    if (!err) err = alloc_err_word();
+    // on the batch stream, complete before the graph can run
+    UBG_CUDA(cudaMemcpyAsync(f.table, host.data(), bytes, cudaMemcpyHostToDevice, st));
+    UBG_CUDA(cudaStreamSynchronize(st));
     long l0 = g_stats.launches;
     cudaGraph_t g = nullptr;
     UBG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
-      for (size_t i = 0; i < slots.size(); i++) {
-        const MultiSlot &sl = slots[i];
-        if (sl.kind == MK_MG || sl.kind == MK_TAIL)
-          launch_multi_mg(sl, d + aoff[i], (const int *)(d + boff[i]), st);
-        else
-          launch_multi_step(sl.kind, d + aoff[i], (const int *)(d + boff[i]), sl.n, sl.blocks, st);
-      }
+      fused_launch(slots, (const char *)f.table, aoff, boff, tag, err, st);
     } catch (...) {
       cudaStreamEndCapture(st, &g);
       if (g) cudaGraphDestroy(g);
@@ -1717,6 +1908,7 @@ struct ubg_batch {
   }
 
   void step(const float *dts, float cfl) {
+    check_fused();
     bool device_dt = dts == nullptr;
     for (size_t i = 0; i < sims.size(); i++) {
       ubg_sim *s = sims[i];
@@ -1751,26 +1943,24 @@ struct ubg_batch {
       return;
     }
     auto k = make_key(device_dt);
-    if (!graph || k != key || cfl_key != cfl) {
-      capture(device_dt, cfl);
-      key = k;
-      cfl_key = cfl;
-    }
+    Branch *b = nullptr;
+    for (auto &c : br)
+      if (c.exec && c.key == k && c.cfl == cfl) b = &c;
+    if (!b) b = &capture(device_dt, cfl);
     for (size_t i = 0; i < sims.size(); i++) UBG_CUDA(cudaStreamWaitEvent(st, pre[i], 0));
-    UBG_CUDA(cudaGraphLaunch(graph, st));
+    UBG_CUDA(cudaGraphLaunch(b->exec, st));
     UBG_CUDA(cudaEventRecord(done, st));
     for (size_t i = 0; i < sims.size(); i++) {
       ubg_sim *s = sims[i];
       UBG_CUDA(cudaStreamWaitEvent(s->st, done, 0));
-      s->fx = after_fx[i];
-      s->fy = after_fy[i];
-      s->mg.cur0 = after_cur0[i];
+      s->fx = b->after_fx[i];
+      s->fy = b->after_fy[i];
+      s->mg.cur0 = b->after_cur0[i];
       s->umax_ready = true;
       s->last_vcycles = s->opt.vcycles;
     }
-    g_stats.launches += graph_launches;
+    g_stats.launches += b->launches;
   }
-  float cfl_key = -1.0f;
 };
 
 int ubg_batch_create(int n, ubg_sim *const *sims, ubg_batch **out) {
@@ -1823,6 +2013,7 @@ int ubg_batch_sync(ubg_batch *b) {
   return guarded([&] {
     if (!b) throw ArgError("null handle");
     UBG_CUDA(cudaStreamSynchronize(b->st));
+    b->check_fused();
     return UBG_OK;
   });
 }

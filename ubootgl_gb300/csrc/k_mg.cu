@@ -616,8 +616,10 @@ __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg
 // One launch over the members of a batch (FP32): block -> member -> tile.
 template <int TX, int TY, int HALO, bool ALPHA1, int NT>
 __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4))
-    k_mg_m(const MgArgs *__restrict__ A, const int *__restrict__ bs, int n) {
+    k_mg_m(const MgArgs *__restrict__ A, const int *__restrict__ bs, int n, unsigned tag,
+           unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   const int m = member_of(bs, n);
   const MgArgs &a = A[m];
   const int l = (int)blockIdx.x - __ldg(bs + m), gx = (a.w + TX - 1) / TX;
@@ -881,8 +883,11 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail(TailArgs<S> a) {
   k_mg_tail_body<S, T>(a);
 }
 // One block per member of a batch (FP32).
-__global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_tail_m(const TailArgs<float> *__restrict__ A) {
+__global__ void __launch_bounds__(TAIL_THREADS, 1)
+    k_mg_tail_m(const TailArgs<float> *__restrict__ A, const int *__restrict__ bs, int n,
+                unsigned tag, unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   k_mg_tail_body<float, float>(A[blockIdx.x]);
 }
 
@@ -1521,7 +1526,9 @@ void mg_alloc(MgHier &mg, int W, int H, float h0) {
     cudaGetLastError();
     throw std::bad_alloc();
   }
-  UBG_CUDA(cudaMemset(arena, 0, total));
+  // zeroed before any stream of the caller uses it
+  UBG_CUDA(cudaMemsetAsync(arena, 0, total, cudaStreamLegacy));
+  UBG_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
   mg_bind(mg, W, H, h0, arena, total);
   mg.arena = arena;
 }
@@ -1734,7 +1741,8 @@ void mg_low_alloc(MgLow &lo, const MgHier &mg, int prec) {
     cudaGetLastError();
     throw std::bad_alloc();
   }
-  UBG_CUDA(cudaMemset(arena, 0, total));
+  UBG_CUDA(cudaMemsetAsync(arena, 0, total, cudaStreamLegacy));
+  UBG_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
   void *host = nullptr;
   if (cudaHostAlloc(&host, sizeof(DcScalars), cudaHostAllocDefault) != cudaSuccess) {
     cudaGetLastError();
@@ -1878,17 +1886,18 @@ void mg_multi_vcycle(const std::vector<MgHier *> &mgs, std::vector<MultiSlot> &o
     if (cur[i][0] != mgs[i]->cur0) throw std::runtime_error("fused V-cycle parity");
 }
 
-void launch_multi_mg(const MultiSlot &slot, const void *dargs, const int *dbs, cudaStream_t st) {
+void launch_multi_mg(const MultiSlot &slot, const void *dargs, const int *dbs, unsigned tag,
+                     unsigned *err, cudaStream_t st) {
   if (slot.kind == MK_TAIL) {
     launch_pdl(k_mg_tail_m, dim3(slot.n), dim3(32, 32), slot.smem, st,
-               (const TailArgs<float> *)dargs);
+               (const TailArgs<float> *)dargs, dbs, slot.n, tag, err);
   } else {
     const MgArgs *A = (const MgArgs *)dargs;
     switch (slot.tile) {
 #define UBG_MULTI_TILE(ID, TX, TY, HALO, NT)                                                   \
   case ID:                                                                                     \
     launch_pdl(k_mg_m<TX, TY, HALO, true, NT>, dim3(slot.blocks), dim3(32, NT / 32),          \
-               Tile<TX, TY, HALO>::smem(4), st, A, dbs, slot.n);                               \
+               Tile<TX, TY, HALO>::smem(4), st, A, dbs, slot.n, tag, err);                     \
     break;
       UBG_MULTI_TILE(0, 112, 50, 8, 512)
       UBG_MULTI_TILE(1, 48, 16, 8, 256)

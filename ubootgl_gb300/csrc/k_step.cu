@@ -714,54 +714,64 @@ inline dim3 grid_vec(int w, int h, int z = 1) {
 
 
 // ---------------------------------------------------- multi-member kernels
-__global__ void k_vbc_m(const VbcM *__restrict__ A, const int *__restrict__ bs, int n) {
+__global__ void k_vbc_m(const VbcM *__restrict__ A, const int *__restrict__ bs, int n,
+        unsigned tag, unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   const int m = member_of(bs, n);
   const VbcM a = A[m];
   k_vbc_body(a.v, a.fx, a.fy, a.bc, a.do_vx, a.do_vy, a.umax, (int)blockIdx.x - __ldg(bs + m), 0, 0);
 }
-__global__ void __launch_bounds__(256) k_diffuse_m(const DiffuseM *__restrict__ A,
-                                                   const int *__restrict__ bs, int n) {
+__global__ void __launch_bounds__(256) k_diffuse_m(const DiffuseM *__restrict__ A, const int *__restrict__ bs, int n,
+            unsigned tag, unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   const int m = member_of(bs, n);
   const DiffuseM a = A[m];
   const int l = (int)blockIdx.x - __ldg(bs + m);
   k_diffuse_body(a.v, a.srcx, a.srcy, a.sc, a.comps, l % a.gx, (l / a.gx) % a.gy, l / (a.gx * a.gy));
 }
-__global__ void __launch_bounds__(256) k_advect_m(const AdvectM *__restrict__ A,
-                                                  const int *__restrict__ bs, int n) {
+__global__ void __launch_bounds__(256) k_advect_m(const AdvectM *__restrict__ A, const int *__restrict__ bs, int n,
+           unsigned tag, unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   const int m = member_of(bs, n);
   const AdvectM a = A[m];
   const int l = (int)blockIdx.x - __ldg(bs + m);
   k_advect_body(a.v, a.srcx, a.srcy, a.sc, l % a.gx, l / a.gx, 0);
 }
-__global__ void __launch_bounds__(256) k_divergence_m(const DivergenceM *__restrict__ A,
-                                                      const int *__restrict__ bs, int n) {
+__global__ void __launch_bounds__(256) k_divergence_m(const DivergenceM *__restrict__ A, const int *__restrict__ bs, int n,
+               unsigned tag, unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   const int m = member_of(bs, n);
   const DivergenceM a = A[m];
   const int l = (int)blockIdx.x - __ldg(bs + m);
   k_divergence_body(a.vx, a.vy, a.f, a.P, a.W, a.H, a.sc, l % a.gx, l / a.gx, 0);
 }
-__global__ void k_pbc_m(const PbcM *__restrict__ A, const int *__restrict__ bs, int n) {
+__global__ void k_pbc_m(const PbcM *__restrict__ A, const int *__restrict__ bs, int n,
+        unsigned tag, unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   const int m = member_of(bs, n);
   const PbcM a = A[m];
   const int l = (int)blockIdx.x - __ldg(bs + m);
   if (l == 0 && threadIdx.x == 0 && a.umax_zero) *a.umax_zero = 0u;
   k_pbc_body(a.p, a.P, a.W, a.H, a.bc, l, 0, 0);
 }
-__global__ void __launch_bounds__(256) k_gradient_m(const GradientM *__restrict__ A,
-                                                    const int *__restrict__ bs, int n) {
+__global__ void __launch_bounds__(256) k_gradient_m(const GradientM *__restrict__ A, const int *__restrict__ bs, int n,
+             unsigned tag, unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   const int m = member_of(bs, n);
   const GradientM a = A[m];
   const int l = (int)blockIdx.x - __ldg(bs + m);
   k_gradient_body(a.v, a.fx, a.fy, a.p, a.sc, a.umax, l % a.gx, l / a.gx, 0);
 }
-__global__ void k_cfl_m(const CflM *__restrict__ A, int n) {
+__global__ void k_cfl_m(const CflM *__restrict__ A, const int *__restrict__ bs, int n, unsigned tag,
+                        unsigned *err) {
   griddep_wait();
+  if (!table_ok(bs, n, tag, err)) return;
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= n) return;
   const CflM a = A[m];
@@ -907,29 +917,30 @@ int multi_blocks_gradient(GradientM &a) {
 }
 
 void launch_multi_step(int kind, const void *args, const int *bs, int n, int blocks,
-                       cudaStream_t st) {
+                       unsigned tag, unsigned *err, cudaStream_t st) {
   switch (kind) {
     case MK_VBC:
-      launch_pdl(k_vbc_m, dim3(blocks), dim3(256), 0, st, (const VbcM *)args, bs, n);
+      launch_pdl(k_vbc_m, dim3(blocks), dim3(256), 0, st, (const VbcM *)args, bs, n, tag, err);
       break;
     case MK_DIFFUSE:
-      launch_pdl(k_diffuse_m, dim3(blocks), dim3(VX, VY), 0, st, (const DiffuseM *)args, bs, n);
+      launch_pdl(k_diffuse_m, dim3(blocks), dim3(VX, VY), 0, st, (const DiffuseM *)args, bs, n, tag, err);
       break;
     case MK_ADVECT:
-      launch_pdl(k_advect_m, dim3(blocks), dim3(BX, BY), 0, st, (const AdvectM *)args, bs, n);
+      launch_pdl(k_advect_m, dim3(blocks), dim3(BX, BY), 0, st, (const AdvectM *)args, bs, n, tag, err);
       break;
     case MK_DIVERGENCE:
       launch_pdl(k_divergence_m, dim3(blocks), dim3(VX, VY), 0, st, (const DivergenceM *)args, bs,
-                 n);
+                 n, tag, err);
       break;
     case MK_PBC:
-      launch_pdl(k_pbc_m, dim3(blocks), dim3(256), 0, st, (const PbcM *)args, bs, n);
+      launch_pdl(k_pbc_m, dim3(blocks), dim3(256), 0, st, (const PbcM *)args, bs, n, tag, err);
       break;
     case MK_GRADIENT:
-      launch_pdl(k_gradient_m, dim3(blocks), dim3(VX, VY), 0, st, (const GradientM *)args, bs, n);
+      launch_pdl(k_gradient_m, dim3(blocks), dim3(VX, VY), 0, st, (const GradientM *)args, bs, n, tag, err);
       break;
     case MK_CFL:
-      launch_pdl(k_cfl_m, dim3((n + 127) / 128), dim3(128), 0, st, (const CflM *)args, n);
+      launch_pdl(k_cfl_m, dim3((n + 127) / 128), dim3(128), 0, st, (const CflM *)args, bs, n, tag,
+                 err);
       break;
     default:
       throw ArgError("multi-member launch kind");

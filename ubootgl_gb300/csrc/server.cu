@@ -1,16 +1,21 @@
 // Step server (extension): continuous batching of step requests over
 // sessions whose fields stay resident on the device.
 //
-// A session is one simulation handle (its own fields, stream and captured
-// step graph).  Sessions are admitted against a device-memory budget when
-// they are opened.  A request asks for k steps of one session.  The worker
-// thread admits queued requests in arrival order whenever a slot is free
-// (at most max_active requests in flight, one per session), enqueues all k
-// steps of an admitted request on its session's stream at once, and polls
-// the streams' completion events: requests that arrive while others run on
-// the GPU join as soon as a slot frees, and the device overlaps the work of
-// every in-flight session.  Sessions touch only their own memory, so a
-// session's result does not depend on what else is in flight.
+// A session is one simulation handle (its own fields and stream).  Sessions
+// are admitted against a device-memory budget when they are opened.  A
+// request asks for k steps of one session.  The worker thread admits queued
+// requests in arrival order whenever a slot is free (one request in flight
+// per session; at most max_active stream requests and 4 * max_active fused
+// requests).  Requests of sessions that the fused form covers (FP32, fixed
+// V-cycle count, at most 1M cells; see FusedStepper) are stepped together:
+// every worker iteration enqueues ONE step of every such request as one
+// launch per kernel over all of them, so a request that arrives joins at
+// the next step boundary and leaves after its k-th step (iteration-level
+// continuous batching, at most two steps in flight).  Other sessions (mixed
+// precision, tolerance mode, larger grids) enqueue their k steps on their
+// own stream.  The worker polls completion events.  Sessions touch only
+// their own memory and the fused step is bit-identical to stepping alone,
+// so a session's result does not depend on what else is in flight.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -18,6 +23,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -33,11 +39,23 @@ double now_ms() {
 }
 }  // namespace
 
+// Sessions up to this many cells are stepped fused by default; larger ones
+// fill the GPU on their own and overlap better as separate streams
+// (measured on GB300: one fused launch per kernel wins by 3x at 128K cells
+// a member and loses ~7 % at 2M).
+constexpr long long kFuseMaxCells = 1LL << 20;
+// A fused request in flight costs one step of a shared launch sequence per
+// worker iteration, not a stream of its own: max_active bounds the stream
+// requests in flight, and kFusedPerSlot * max_active the fused ones.
+constexpr int kFusedPerSlot = 4;
+// Steps of a stream request enqueued at a time (at most two chunks queued).
+constexpr int kChunkSteps = 2;
+
 struct ubg_server {
   struct Session {
     ubg_sim *sim = nullptr;
     cudaStream_t st = nullptr;
-    cudaEvent_t ev = nullptr;
+    cudaEvent_t evc[2] = {nullptr, nullptr};  // completion of queued work
     size_t bytes = 0;
     long long cells = 0;
     bool busy = false;
@@ -47,12 +65,18 @@ struct ubg_server {
     int steps = 0;
     float cfl = 0.5f;
     double t_submit = 0, t_admit = 0, t_end = 0;
+    bool fused = false;  // stepped by the fused stepper
+    int remaining = 0;   // fused steps not yet enqueued
+    int enq = 0;         // stream steps enqueued so far
+    int chunks = 0;      // stream chunks enqueued so far
     bool finished = false;
     int error = 0;
   };
 
   size_t budget = 0, used = 0;
   int max_active = 1;
+  int mode = UBG_SERVE_FUSED;
+  long long fuse_max_cells = kFuseMaxCells;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::map<int, Session> sessions;
@@ -63,15 +87,100 @@ struct ubg_server {
   std::vector<uint64_t> active;
   std::vector<double> latencies;
   long long rejected = 0, cell_steps = 0, completed = 0;
+  long long fused_steps = 0, fused_member_steps = 0;
+  double worker_fused_ms = 0.0, worker_streams_ms = 0.0;
   double t_first = -1.0, t_last = 0.0;
   bool stop = false;
+  std::unique_ptr<FusedStepper> fs;
   std::thread worker;
+
+  // Enqueues the next chunk of a stream request's steps once at most one
+  // chunk is still queued (chunk i records evc[i % 2]).  Keeping only a few
+  // steps queued per session keeps the worker out of a full launch queue,
+  // where every launch would block it.
+  int stream_topup(Request &r, Session &s) {
+    if (r.enq >= r.steps) return UBG_OK;
+    if (r.chunks >= 2) {
+      cudaError_t q = cudaEventQuery(s.evc[r.chunks % 2]);
+      if (q == cudaErrorNotReady) return UBG_OK;
+      if (q != cudaSuccess) {
+        cudaGetLastError();
+        return UBG_ECUDA;
+      }
+    }
+    const double t0 = now_ms();
+    const int n = std::min(kChunkSteps, r.steps - r.enq);
+    int rc = UBG_OK;
+    for (int k = 0; k < n && rc == UBG_OK; k++) rc = ubg_step_cfl(s.sim, r.cfl);
+    if (rc == UBG_OK && cudaEventRecord(s.evc[r.chunks % 2], s.st) != cudaSuccess) rc = UBG_ECUDA;
+    r.enq += n;
+    r.chunks++;
+    worker_streams_ms += now_ms() - t0;
+    return rc;
+  }
+
+  void fail(Request &r, Session &s, int code) {
+    r.t_end = now_ms();
+    r.finished = true;
+    r.error = code;
+    s.busy = false;
+    cv_done.notify_all();
+  }
+
+  // One fused step of every fused request with steps left (grouped by
+  // V-cycle count); requests whose last step was enqueued start draining.
+  bool fused_tick() {
+    std::map<int, std::vector<uint64_t>> groups;
+    for (uint64_t id : active) {
+      Request &r = reqs[id];
+      if (r.fused && r.remaining > 0) groups[FusedStepper::group(sessions[r.session].sim)].push_back(id);
+    }
+    if (groups.empty() || !fs->ready()) return false;
+    const double t0 = now_ms();
+    for (auto &g : groups) {
+      std::vector<ubg_sim *> sims;
+      std::vector<float> cfl;
+      for (uint64_t id : g.second) {
+        sims.push_back(sessions[reqs[id].session].sim);
+        cfl.push_back(reqs[id].cfl);
+      }
+      try {
+        fs->step(sims, cfl);
+        fused_steps++;
+        fused_member_steps += (long long)g.second.size();
+        for (uint64_t id : g.second) {
+          Request &r = reqs[id];
+          if (--r.remaining == 0) {
+            Session &ses = sessions[r.session];
+            fs->leave(ses.sim, ses.evc[0]);
+          }
+        }
+      } catch (const std::exception &e) {
+        set_last_error(e.what());
+        cudaGetLastError();
+        for (uint64_t id : g.second) {
+          Request &r = reqs[id];
+          r.remaining = 0;
+          fail(r, sessions[r.session], UBG_ECUDA);
+        }
+        active.erase(std::remove_if(active.begin(), active.end(),
+                                    [&](uint64_t id) { return reqs[id].finished; }),
+                     active.end());
+      }
+    }
+    worker_fused_ms += now_ms() - t0;
+    return true;
+  }
 
   void run() {
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
       // admit in arrival order while slots are free
-      for (auto it = queue.begin(); it != queue.end() && (int)active.size() < max_active;) {
+      int n_fused = 0;
+      for (uint64_t id : active) n_fused += reqs[id].fused;
+      int n_streams = (int)active.size() - n_fused;
+      for (auto it = queue.begin();
+           it != queue.end() && (n_streams < max_active || n_fused < kFusedPerSlot * max_active);) {
         Request &r = reqs[*it];
         auto sit = sessions.find(r.session);
         if (sit == sessions.end()) {  // session closed before admission
@@ -82,26 +191,37 @@ struct ubg_server {
           continue;
         }
         Session &s = sit->second;
-        if (s.busy) {
+        const bool fuse = mode == UBG_SERVE_FUSED && s.cells <= fuse_max_cells &&
+                          FusedStepper::eligible(s.sim);
+        if (s.busy || (fuse ? n_fused >= kFusedPerSlot * max_active : n_streams >= max_active)) {
           ++it;
           continue;
         }
         s.busy = true;
         r.t_admit = now_ms();
         if (t_first < 0.0) t_first = r.t_admit;
-        // enqueue every step of the request on the session's stream
         int rc = UBG_OK;
-        for (int k = 0; k < r.steps && rc == UBG_OK; k++) rc = ubg_step_cfl(s.sim, r.cfl);
-        if (rc == UBG_OK && cudaEventRecord(s.ev, s.st) != cudaSuccess) rc = UBG_ECUDA;
+        if (fuse) {
+          try {
+            if (!fs) fs.reset(new FusedStepper());
+            fs->join(s.sim);
+            r.fused = true;
+            r.remaining = r.steps;
+          } catch (const std::exception &e) {
+            set_last_error(e.what());
+            cudaGetLastError();
+            rc = UBG_ECUDA;
+          }
+        } else {
+          rc = stream_topup(r, s);
+        }
         if (rc != UBG_OK) {
-          r.finished = true;
-          r.error = rc;
-          s.busy = false;
+          fail(r, s, rc);
           it = queue.erase(it);
-          cv_done.notify_all();
           continue;
         }
         active.push_back(*it);
+        (fuse ? n_fused : n_streams)++;
         it = queue.erase(it);
       }
       if (active.empty()) {
@@ -109,20 +229,41 @@ struct ubg_server {
         cv_work.wait(lk);
         continue;
       }
-      // completion polling
+      bool stepped = fused_tick();
+      // stream top-ups and completion polling
       bool any = false;
       for (size_t i = 0; i < active.size();) {
         Request &r = reqs[active[i]];
         Session &s = sessions[r.session];
-        cudaError_t q = cudaEventQuery(s.ev);
-        if (q == cudaErrorNotReady) {
+        if (r.fused && r.remaining > 0) {
           i++;
           continue;
+        }
+        cudaError_t q = cudaSuccess;
+        if (!r.fused && r.enq < r.steps) {
+          const int c0 = r.chunks;
+          if (stream_topup(r, s) != UBG_OK) {
+            q = cudaErrorUnknown;
+          } else {
+            stepped |= r.chunks != c0;
+            i++;
+            continue;
+          }
+        } else {
+          // the request's last work: the stepper's event, or its last chunk
+          q = cudaEventQuery(r.fused ? s.evc[0] : s.evc[(r.chunks - 1) % 2]);
+          if (q == cudaErrorNotReady) {
+            i++;
+            continue;
+          }
         }
         r.t_end = now_ms();
         r.finished = true;
         if (q != cudaSuccess) {
           cudaGetLastError();
+          r.error = UBG_ECUDA;
+        } else if (r.fused && fs->failed()) {
+          set_last_error("fused step: a launch found a table it was not made for");
           r.error = UBG_ECUDA;
         }
         s.busy = false;
@@ -135,7 +276,7 @@ struct ubg_server {
       }
       if (any) {
         cv_done.notify_all();
-      } else {
+      } else if (!stepped) {
         lk.unlock();
         std::this_thread::sleep_for(std::chrono::microseconds(20));
         lk.lock();
@@ -174,12 +315,28 @@ int ubg_server_destroy(ubg_server *s) {
   }
   s->cv_work.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  s->fs.reset();
   for (auto &kv : s->sessions) {
-    cudaEventDestroy(kv.second.ev);
+    for (cudaEvent_t e : kv.second.evc) cudaEventDestroy(e);
     ubg_destroy(kv.second.sim);
   }
   delete s;
   set_last_error("");
+  return UBG_OK;
+}
+
+int ubg_server_set_mode(ubg_server *s, int mode) {
+  if (!s || (mode != UBG_SERVE_STREAMS && mode != UBG_SERVE_FUSED))
+    return srv_fail(UBG_EINVAL, "bad argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->mode = mode;
+  return UBG_OK;
+}
+
+int ubg_server_set_fuse_cells(ubg_server *s, long long max_cells) {
+  if (!s || max_cells < 0) return srv_fail(UBG_EINVAL, "bad argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->fuse_max_cells = max_cells;
   return UBG_OK;
 }
 
@@ -217,12 +374,15 @@ int ubg_server_open(ubg_server *s, const float *flag, int width, int height, flo
     void *st = nullptr;
     ubg_stream(sim, &st);
     ses.st = (cudaStream_t)st;
-    if (cudaEventCreateWithFlags(&ses.ev, cudaEventDisableTiming) != cudaSuccess) {
-      cudaGetLastError();
-      rc = srv_fail(UBG_ECUDA, "event creation failed");
-    }
+    for (cudaEvent_t &e : ses.evc)
+      if (rc == UBG_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        rc = srv_fail(UBG_ECUDA, "event creation failed");
+      }
   }
   if (rc != UBG_OK) {
+    for (cudaEvent_t e : ses.evc)
+      if (e) cudaEventDestroy(e);
     if (sim) ubg_destroy(sim);
     unreserve();
     return rc;
@@ -251,7 +411,8 @@ int ubg_server_close(ubg_server *s, int session) {
     s->sessions.erase(it);
     s->used -= ses.bytes;
   }
-  cudaEventDestroy(ses.ev);
+  for (cudaEvent_t e : ses.evc)
+    if (e) cudaEventDestroy(e);
   ubg_destroy(ses.sim);
   return UBG_OK;
 }
@@ -314,6 +475,10 @@ int ubg_server_stats(ubg_server *s, ubg_serve_stats *out) {
   out->cell_steps = s->cell_steps;
   out->device_bytes_used = s->used;
   out->busy_ms = s->t_first < 0.0 ? 0.0 : s->t_last - s->t_first;
+  out->fused_steps = s->fused_steps;
+  out->fused_member_steps = s->fused_member_steps;
+  out->worker_fused_ms = s->worker_fused_ms;
+  out->worker_streams_ms = s->worker_streams_ms;
   if (!s->latencies.empty()) {
     std::vector<double> v = s->latencies;
     std::sort(v.begin(), v.end());

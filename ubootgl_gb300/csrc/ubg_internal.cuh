@@ -265,6 +265,18 @@ __device__ __forceinline__ int member_of(const int *__restrict__ bs, int n) {
   return lo;
 }
 
+// Every fused launch first checks its table: the word after the member
+// prefix sums, bs[n + 1], must equal the launch's tag (written with the
+// table).  A launch that finds another value (a table not yet written, or
+// not the one the launch was made for) sets *err and returns without
+// touching any field.
+__device__ __forceinline__ bool table_ok(const int *__restrict__ bs, int n, unsigned tag,
+                                         unsigned *err) {
+  if ((unsigned)__ldg(bs + n + 1) == tag) return true;
+  if (threadIdx.x == 0 && threadIdx.y == 0) atomicOr(err, 1u);
+  return false;
+}
+
 // One launch of a fused batch step: `n` members, their argument structs
 // back to back, the block prefix sums and the dynamic shared memory.
 struct MultiSlot {
@@ -285,7 +297,7 @@ int multi_blocks_pbc(const PbcM &a);
 int multi_blocks_gradient(GradientM &a);
 // Launches over n members (device tables args, bs; total blocks).
 void launch_multi_step(int kind, const void *args, const int *bs, int n, int blocks,
-                       cudaStream_t st);
+                       unsigned tag, unsigned *err, cudaStream_t st);
 
 // ------------------------------------------------------------ multigrid
 struct MgLevel {
@@ -325,7 +337,8 @@ void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report);
 // smoother tile.  Every member needs a coarse tail (tail_top >= 1).
 void mg_multi_vcycle(const std::vector<MgHier *> &mgs, std::vector<MultiSlot> &out);
 // Launches one MK_MG / MK_TAIL slot whose tables are at dargs / dbs.
-void launch_multi_mg(const MultiSlot &slot, const void *dargs, const int *dbs, cudaStream_t st);
+void launch_multi_mg(const MultiSlot &slot, const void *dargs, const int *dbs, unsigned tag,
+                     unsigned *err, cudaStream_t st);
 
 // Allocates the hierarchy for a W x H level-0 grid with spacing h0.
 void mg_alloc(MgHier &mg, int W, int H, float h0);
@@ -461,6 +474,42 @@ struct ProfScope {
       p->marks.push_back({kc, a, b});
     }
   }
+};
+
+// Steps a changing set of simulations together, one launch per kernel over
+// the whole set per step (continuous batching).  The work runs on the
+// stepper's own stream, in order; members join and leave between steps.
+// The members must be eligible(): FP32, fixed V-cycle count, a coarse
+// tail, no sinks, not profiling.  Each member's results are bit-identical
+// to stepping it alone.
+class FusedStepper {
+ public:
+  FusedStepper();
+  ~FusedStepper();
+  FusedStepper(const FusedStepper &) = delete;
+  FusedStepper &operator=(const FusedStepper &) = delete;
+  static bool eligible(const ubg_sim *s);
+  // Members stepped together need the same group (their V-cycle count).
+  static int group(const ubg_sim *s);
+  // Orders the stepper's stream after the work on s's stream so far and
+  // readies s's dt input (pending staged input, accumulation, max|u|).
+  void join(ubg_sim *s);
+  // True when the next step can be enqueued without waiting on the device
+  // (at most two steps in flight).
+  bool ready() const;
+  // One device-CFL step of every member; cfl[i] is member i's factor.  The
+  // members need the same V-cycle count.
+  void step(const std::vector<ubg_sim *> &sims, const std::vector<float> &cfl);
+  // Records ev on the stepper's stream after s's last fused step and makes
+  // s's own stream wait for it.
+  void leave(ubg_sim *s, cudaEvent_t ev);
+  // True once a fused launch found a table it was not made for (that
+  // launch skipped its work); read after the steps in question completed.
+  bool failed() const;
+
+ private:
+  struct Impl;
+  Impl *p_;
 };
 
 }  // namespace ubg

@@ -272,11 +272,18 @@ class Batch:
 class Server:
     """Step server over resident sessions (extension; ubg_server_*)."""
 
-    def __init__(self, budget_bytes, max_active=16):
+    def __init__(self, budget_bytes, max_active=16, mode="fused", fuse_cells=None):
+        """mode "fused": one step of every in-flight FP32 request of at most
+        `fuse_cells` cells (library default 2^20) per launch sequence
+        (continuous batching); "streams": each request's steps on its
+        session's own stream."""
         self._lib = L.load()
         h = C.c_void_p()
         L.check(self._lib.ubg_server_create(int(budget_bytes), int(max_active), C.byref(h)))
         self._h = h
+        L.check(self._lib.ubg_server_set_mode(h, {"streams": 0, "fused": 1}[mode]))
+        if fuse_cells is not None:
+            L.check(self._lib.ubg_server_set_fuse_cells(h, int(fuse_cells)))
 
     def open(self, flag, vx=None, vy=None, pwidth=1.0, mu=1e-4, precision="fp32", vcycles=2):
         """Returns the session id, or None when the memory budget rejects it."""
