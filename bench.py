@@ -260,6 +260,9 @@ def run_ours(args):
     if args.batch > 0:
         for prec in args.batch_precisions.split(","):
             batched[prec] = batch_bench(L, lib, args.batch, args.batch_steps, args.warmup, prec)
+        # small members, where one launch per kernel over the batch pays most
+        batched["fp32_small"] = batch_bench(L, lib, args.batch, args.batch_steps, args.warmup,
+                                            "fp32", wmin=128, wmax=512)
     if args.serve_sessions > 0:
         for prec in args.serve_precisions.split(","):
             for mode in args.serve_modes.split(","):
@@ -347,16 +350,16 @@ def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev):
                       "solve" % precision, "fields_finite": finite}
 
 
-def batch_bench(L, lib, n, steps, warmup, precision, seed=11):
+def batch_bench(L, lib, n, steps, warmup, precision, seed=11, wmin=128, wmax=2048):
     """Batched uneven instances: n simulations, widths log-uniform in
-    [128, 2048] (multiples of 32), height = width / 2, each with its own
+    [wmin, wmax] (multiples of 32), height = width / 2, each with its own
     seeded disc mask (8-15 % solid) and inflow speed (uniform [0.5, 1.5]);
     every member autotuned; all advance one step per batch graph launch.
     Host wall clock around K batch steps (synchronised), against the same
     members stepped one call each on their own streams."""
     from ubootgl_gb300 import workload as WL
     from ubootgl_gb300.simulation import Batch, Simulation
-    widths = WL.log_uniform_widths(n, 128, 2048, seed)
+    widths = WL.log_uniform_widths(n, wmin, wmax, seed)
     sims, cells = [], 0
     for i, W in enumerate(widths):
         H = W // 2
@@ -399,7 +402,8 @@ def batch_bench(L, lib, n, steps, warmup, precision, seed=11):
             "ms_per_batch_step": round(1e3 * t_batch / steps, 4),
             "one_call_per_member_value": round(cells * steps / t_seq / 1e6, 2),
             "autotune_s": round(t_tune, 2), "precision": precision, "fields_finite": finite,
-            "widths": "log-uniform [128, 2048], h = w/2", "timing": "host wall clock, synchronised"}
+            "widths": "log-uniform [%d, %d], h = w/2" % (wmin, wmax),
+            "timing": "host wall clock, synchronised"}
 
 
 def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, precision, mode,

@@ -235,13 +235,14 @@ int ubg_restore(ubg_sim *sim, const void *src);
 int ubg_autotune(ubg_sim *sim, char *report, size_t len);
 
 /* Batch (extension): n independent simulations of any sizes advanced
- * together, one CUDA graph launch per batch step.  When every member is
- * FP32 with dt from the device and the members average under 1.5 M cells,
- * the step is fused: each kernel of the step is one launch over all members
- * (blocks mapped to members through prefix sums, per-member arguments in a
- * device table), ~40 launches whatever the member count.  Otherwise the
- * graph's parallel branches are the members' own step bodies.  dts: n host time steps, or NULL for dt = cfl * h / max|u|
- * per member on the device.  Members keep their own fields, options and
+ * together, one CUDA graph launch per batch step.  With dt from the device,
+ * the FP32 fixed-mode members of at most 2^20 cells (at least two of them)
+ * are fused: each kernel of the step is one launch over all of them (blocks
+ * mapped to members through prefix sums, per-member arguments in a device
+ * table), ~40 launches whatever their count.  The other members' own step
+ * bodies run as parallel branches of the same graph.  dts: n host time
+ * steps (every member then a branch), or NULL for dt = cfl * h / max|u| per
+ * member on the device.  Members keep their own fields, options and
  * streams (ordered after the batch step); each member's result is
  * bit-identical to stepping it alone.  Members need UBG_SOLVE_FIXED and no
  * pending sinks.  The batch does not own the members. */

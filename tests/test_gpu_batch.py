@@ -1,11 +1,12 @@
 """Batches and the autotuner: results identical to stepping alone.
 
-A batch step captures every member's fixed-cycle step body as a parallel
-branch of one CUDA graph; the members only touch their own memory and the
-arithmetic is the single-simulation path, so each member must be
-bit-identical to the same simulation stepped alone (tolerance 0).  The
-autotuner only changes tile shapes and the coarse-tail size, which must not
-change a bit either.
+A batch step is one CUDA graph: small FP32 members are stepped by fused
+launches (one launch per kernel over all of them), the other members'
+fixed-cycle step bodies are parallel branches.  The members only touch
+their own memory and every kernel runs the single-simulation arithmetic, so
+each member must be bit-identical to the same simulation stepped alone
+(tolerance 0).  The autotuner only changes tile shapes and the coarse-tail
+size, which must not change a bit either.
 """
 import numpy as np
 import pytest
@@ -122,6 +123,29 @@ def test_fused_batch_uneven_many(lib):
         if it == 2:
             alone[3].step_cfl(0.5)
             members[3].step_cfl(0.5)
+        for s in alone:
+            s.step_cfl(0.5)
+        batch.step(cfl=0.5)
+    batch.sync()
+    for a, b in zip(alone, members):
+        for n in ("vx", "vy", "vx_back", "vy_back", "p"):
+            assert np.array_equal(a.get(n), b.get(n)), (a.width, n)
+    batch.close()
+    for s in alone + members:
+        s.close()
+
+
+def test_hybrid_batch_fused_and_branches(lib):
+    """Small FP32 members fused, a member above 2^20 cells and a mixed-
+    precision member as graph branches of the same batch step: all
+    bit-identical to stepping alone."""
+    from ubootgl_gb300.simulation import Batch
+    cfg = [(1536, 768, "fp32"), (128, 64, "fp32"), (256, 128, "fp16"), (320, 160, "fp32"),
+           (96, 48, "fp32")]
+    alone = [build(W, H, 400 + i, p, 0.6 + 0.1 * i) for i, (W, H, p) in enumerate(cfg)]
+    members = [build(W, H, 400 + i, p, 0.6 + 0.1 * i) for i, (W, H, p) in enumerate(cfg)]
+    batch = Batch(members)
+    for _ in range(4):
         for s in alone:
             s.step_cfl(0.5)
         batch.step(cfl=0.5)

@@ -1743,7 +1743,7 @@ struct ubg_batch {
     std::vector<long long> key;
     cudaGraphExec_t exec = nullptr;
     void *table = nullptr;
-    std::vector<int> after_fx, after_fy;
+    std::vector<int> after_fx, after_fy, after_cur0;
     long launches = 0;
   };
   Fused fused[2];
@@ -1841,22 +1841,31 @@ struct ubg_batch {
     return b;
   }
 
-  // The fused form needs FP32 members in fixed mode with a coarse tail and
-  // a device-side dt; anything else takes the per-member branches.
-  // Measured on GB300: fused launches win by far for small members (64 x
-  // 128x64: 0.24 vs 3.9 ms per batch step; 64 x 512x256: 1.8 vs 5.6 ms);
-  // members of 2 M cells run ~7 % faster as concurrent graph branches.
-  bool fusable(bool device_dt) const {
+  // Members the fused launches take: FP32, fixed V-cycle count, a coarse
+  // tail, at most kFuseMaxCells cells; the others become graph branches of
+  // the same step.  Measured on GB300: fused launches win by far for small
+  // members (64 x 128x64: 0.24 vs 3.9 ms per batch step; 64 x 512x256: 1.8
+  // vs 5.6 ms); members of 2 M cells run ~7 % faster as concurrent
+  // branches.  The fused form needs a device-side dt and two small members.
+  bool partition(bool device_dt, std::vector<int> &small, std::vector<int> &big) const {
+    small.clear();
+    big.clear();
     if (!use_fused || !device_dt) return false;
-    double cells = 0.0;
-    for (auto *s : sims) {
-      if (s->opt.precision != UBG_FP32 || s->mg.tail_top < 1 || s->opt.vcycles < 1) return false;
-      cells += (double)s->W * s->H;
+    const int vc = sims[0]->opt.vcycles;
+    for (size_t i = 0; i < sims.size(); i++) {
+      ubg_sim *s = sims[i];
+      if (FusedStepper::eligible(s) && s->opt.vcycles == vc &&
+          (long long)s->W * s->H <= kFuseMaxCells)
+        small.push_back((int)i);
+      else
+        big.push_back((int)i);
     }
-    return cells / (double)sims.size() < 1.5e6;
+    return small.size() >= 2;
   }
 
-  Fused &fused_graph(float cfl) {
+  // One graph per index state: fused launches over the small members on
+  // the batch stream, the big members' step bodies as branches beside them.
+  Fused &fused_graph(float cfl, const std::vector<int> &small, const std::vector<int> &big) {
     std::vector<long long> k = make_key(true);
     k.push_back((long long)__builtin_bit_cast(unsigned, cfl));
     for (auto &f : fused)
@@ -1872,9 +1881,21 @@ struct ubg_batch {
       cudaFree(f.table);
       f.table = nullptr;
     }
+    const size_t n = sims.size();
+    f.after_fx.assign(n, 0);
+    f.after_fy.assign(n, 0);
+    f.after_cur0.assign(n, 0);
+    std::vector<ubg_sim *> ss;
+    for (int i : small) ss.push_back(sims[i]);
     std::vector<MultiSlot> slots;
-    std::vector<float> cfls(sims.size(), cfl);
-    fused_plan(sims, cfls.data(), slots, f.after_fx, f.after_fy);
+    std::vector<float> cfls(ss.size(), cfl);
+    std::vector<int> afx, afy;
+    fused_plan(ss, cfls.data(), slots, afx, afy);
+    for (size_t j = 0; j < small.size(); j++) {
+      f.after_fx[small[j]] = afx[j];
+      f.after_fy[small[j]] = afy[j];
+      f.after_cur0[small[j]] = ss[j]->mg.cur0;
+    }
     std::vector<char> host;
     std::vector<size_t> aoff, boff;
     const unsigned tag = fused_tag();
@@ -1889,15 +1910,43 @@ struct ubg_batch {
     UBG_CUDA(cudaMemcpyAsync(f.table, host.data(), bytes, cudaMemcpyHostToDevice, st));
     UBG_CUDA(cudaStreamSynchronize(st));
     long l0 = g_stats.launches;
+    std::vector<int> fx0(n), fy0(n), c00(n);
+    for (size_t i = 0; i < n; i++) {
+      fx0[i] = sims[i]->fx;
+      fy0[i] = sims[i]->fy;
+      c00[i] = sims[i]->mg.cur0;
+    }
+    auto restore = [&] {
+      for (size_t i = 0; i < n; i++) {
+        sims[i]->fx = fx0[i];
+        sims[i]->fy = fy0[i];
+        sims[i]->mg.cur0 = c00[i];
+      }
+    };
     cudaGraph_t g = nullptr;
     UBG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
+      if (!big.empty()) UBG_CUDA(cudaEventRecord(fork, st));
+      for (int i : big) {
+        ubg_sim *s = sims[i];
+        UBG_CUDA(cudaStreamWaitEvent(s->st, fork, 0));
+        launch_cfl(s->v, s->fx, s->fy, cfl, s->h, s->mu, s->pwidth, s->d_umax, s->d_sc, s->st,
+                   true);
+        s->step_body(0);
+        UBG_CUDA(cudaEventRecord(join[i], s->st));
+        f.after_fx[i] = s->fx;
+        f.after_fy[i] = s->fy;
+        f.after_cur0[i] = s->mg.cur0;
+      }
       fused_launch(slots, (const char *)f.table, aoff, boff, tag, err, st);
+      for (int i : big) UBG_CUDA(cudaStreamWaitEvent(st, join[i], 0));
     } catch (...) {
       cudaStreamEndCapture(st, &g);
       if (g) cudaGraphDestroy(g);
+      restore();
       throw;
     }
+    restore();
     UBG_CUDA(cudaStreamEndCapture(st, &g));
     UBG_CUDA(cudaGraphInstantiate(&f.exec, g, 0));
     cudaGraphDestroy(g);
@@ -1926,8 +1975,9 @@ struct ubg_batch {
                    false);
       UBG_CUDA(cudaEventRecord(pre[i], s->st));
     }
-    if (fusable(device_dt)) {
-      Fused &f = fused_graph(cfl);
+    std::vector<int> small, big;
+    if (partition(device_dt, small, big)) {
+      Fused &f = fused_graph(cfl, small, big);
       for (size_t i = 0; i < sims.size(); i++) UBG_CUDA(cudaStreamWaitEvent(st, pre[i], 0));
       UBG_CUDA(cudaGraphLaunch(f.exec, st));
       UBG_CUDA(cudaEventRecord(done, st));
@@ -1936,6 +1986,7 @@ struct ubg_batch {
         UBG_CUDA(cudaStreamWaitEvent(s->st, done, 0));
         s->fx = f.after_fx[i];
         s->fy = f.after_fy[i];
+        s->mg.cur0 = f.after_cur0[i];
         s->umax_ready = true;
         s->last_vcycles = s->opt.vcycles;
       }

@@ -39,11 +39,6 @@ double now_ms() {
 }
 }  // namespace
 
-// Sessions up to this many cells are stepped fused by default; larger ones
-// fill the GPU on their own and overlap better as separate streams
-// (measured on GB300: one fused launch per kernel wins by 3x at 128K cells
-// a member and loses ~7 % at 2M).
-constexpr long long kFuseMaxCells = 1LL << 20;
 // A fused request in flight costs one step of a shared launch sequence per
 // worker iteration, not a stream of its own: max_active bounds the stream
 // requests in flight, and kFusedPerSlot * max_active the fused ones.

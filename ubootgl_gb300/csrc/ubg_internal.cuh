@@ -476,6 +476,10 @@ struct ProfScope {
   }
 };
 
+// Largest member (in cells) that fused launches take by default; larger
+// grids fill the GPU on their own and overlap better as separate streams.
+constexpr long long kFuseMaxCells = 1LL << 20;
+
 // Steps a changing set of simulations together, one launch per kernel over
 // the whole set per step (continuous batching).  The work runs on the
 // stepper's own stream, in order; members join and leave between steps.
