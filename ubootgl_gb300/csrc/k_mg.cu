@@ -436,70 +436,98 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   }
 
   // ---- red-black sweeps: a thread updates 4 consecutive cells of one colour
-  // in one row (128-bit shared-memory accesses); G threads cover a row.
-  constexpr int G = HX / 4, RPP = NT / G;
-  static_assert(HX % 4 == 0 && NT % G == 0, "vector layout");
-  const int k0 = 4 * (tid % G), rsub = tid / G;
+  // in one row (128-bit shared-memory accesses); G threads cover a row.  A
+  // warp covers R = 32 / G rows two apart and its partner warp the rows in
+  // between, so a row's parity is the same across a warp and, because a
+  // pass covers an even number of rows, fixed for a thread through a half
+  // sweep: the parity-dependent selects become two specialised loops.
+  constexpr int G = HX / 4, R = 32 / G, RPP = NT / G;
+  static_assert(HX % 4 == 0 && NT % G == 0 && 32 % G == 0 && (NT / 32) % 2 == 0,
+                "vector layout");
+  const int lane = tid & 31, wid = tid >> 5;
+  const int k0 = 4 * (lane % G);
+  const int rsub = (wid >> 1) * (2 * R) + (wid & 1) + 2 * (lane / G);
   const float hh = a.hh;
   const bool inner = x0 >= 1 && y0 >= 1 && x0 + RX <= w - 1 && y0 + RY <= h - 1;
-  // which of the thread's 4 cells may be smoothed (both parities):
-  // k >= 1 - par and k <= HX - 1 - par keep all neighbours in the region
-  auto cell_ok = [&](int k, int par, int gy) {
-    bool ok = k >= 1 - par && k <= HX - 1 - par;
-    if (!inner) {
-      int gx = x0 + 2 * k + par;
-      ok = ok && gx >= 1 && gx < w - 1 && gy >= 1 && gy < h - 1;
+  // which of the thread's 4 cells may be smoothed, per row parity: k >= 1 -
+  // par and k <= HX - 1 - par keep all neighbours in the region; the column
+  // must be inside the domain's interior
+  unsigned cmask[2];
+#pragma unroll
+  for (int par = 0; par < 2; par++) {
+    unsigned m = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int k = k0 + j, gx = x0 + 2 * k + par;
+      const bool ok = k >= 1 - par && k <= HX - 1 - par && gx >= 1 && gx < w - 1;
+      m |= ok ? (1u << j) : 0u;
     }
-    return ok;
+    cmask[par] = m;
+  }
+  auto sweep = [&](auto parc, const int color, const int half) {
+    constexpr int PAR = decltype(parc)::value;
+    S *self = sp + color * RY * HX;
+    const S *oth = sp + (color ^ 1) * RY * HX;
+    const S *fs = sf + color * RY * HX;
+    const uint8_t *cs = sc + color * RY * HX;
+    const unsigned cm = cmask[PAR];
+    for (int ry = half + rsub; ry <= RY - 1 - half; ry += RPP) {
+      if (!inner) {
+        const int gy = y0 + ry;
+        if (gy < 1 || gy >= h - 1) continue;  // boundary row: kept as it is
+      }
+      const int row = ry * HX + k0;
+      const float4 o = St::lds4(oth + row);
+      const float ex = St::tof(PAR ? oth[row + 4] : oth[row - 1]);
+      const float4 os = St::lds4(oth + row - HX);
+      const float4 on = St::lds4(oth + row + HX);
+      const float4 fv = St::lds4(fs + row);
+      const unsigned cw = *reinterpret_cast<const unsigned *>(cs + row);
+      const float W4[4] = {PAR ? o.x : ex, PAR ? o.y : o.x, PAR ? o.z : o.y, PAR ? o.w : o.z};
+      const float E4[4] = {PAR ? o.y : o.x, PAR ? o.z : o.y, PAR ? o.w : o.z, PAR ? ex : o.w};
+      const float S4[4] = {os.x, os.y, os.z, os.w}, N4[4] = {on.x, on.y, on.z, on.w};
+      const float F4[4] = {fv.x, fv.y, fv.z, fv.w};
+      float out[4];
+      if (ALPHA1) {
+        // warp-uniform choice: all-fluid neighbourhoods take val / 4
+        if (__all_sync(__activemask(), cw == 0x1f1f1f1fu)) {
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            out[j] = ((((W4[j] + E4[j]) + S4[j]) + N4[j]) + F4[j] * hh * hh) * 0.25f;
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            out[j] = rb_update1((cw >> (8 * j)) & 0xffu, W4[j], E4[j], S4[j], N4[j], F4[j], hh);
+        }
+        if (cm != 0xfu) {  // edge columns keep their values
+          const float4 sv = St::lds4(self + row);
+          const float P4[4] = {sv.x, sv.y, sv.z, sv.w};
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            if (!((cm >> j) & 1u)) out[j] = P4[j];
+        }
+      } else {
+        const float4 sv = St::lds4(self + row);
+        const float P4[4] = {sv.x, sv.y, sv.z, sv.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          out[j] = ((cm >> j) & 1u) ? rb_update_alpha((cw >> (8 * j)) & 0xffu, P4[j], W4[j], E4[j],
+                                                      S4[j], N4[j], F4[j], hh, a.alpha)
+                                    : P4[j];
+      }
+      St::sts4(self + row, make_float4(out[0], out[1], out[2], out[3]));
+    }
   };
   int half = 0;
   for (int s = 0; s < a.nsweeps; s++) {
 #pragma unroll
     for (int color = 1; color >= 0; color--) {
       half++;
-      S *self = sp + color * RY * HX;
-      const S *oth = sp + (color ^ 1) * RY * HX;
-      const S *fs = sf + color * RY * HX;
-      const uint8_t *cs = sc + color * RY * HX;
-      for (int ry = half + rsub; ry <= RY - 1 - half; ry += RPP) {
-        const int par = (ry + color) & 1;
-        const int gy = y0 + ry;
-        const int row = ry * HX + k0;
-        const float4 o = St::lds4(oth + row);
-        const float ex = St::tof(par ? oth[row + 4] : oth[row - 1]);
-        const float4 os = St::lds4(oth + row - HX);
-        const float4 on = St::lds4(oth + row + HX);
-        const float4 fv = St::lds4(fs + row);
-        const float4 sv = St::lds4(self + row);
-        const uchar4 cv = *reinterpret_cast<const uchar4 *>(cs + row);
-        const float W4[4] = {par ? o.x : ex, par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z};
-        const float E4[4] = {par ? o.y : o.x, par ? o.z : o.y, par ? o.w : o.z, par ? ex : o.w};
-        const float S4[4] = {os.x, os.y, os.z, os.w}, N4[4] = {on.x, on.y, on.z, on.w};
-        const float F4[4] = {fv.x, fv.y, fv.z, fv.w}, P4[4] = {sv.x, sv.y, sv.z, sv.w};
-        const unsigned C4[4] = {cv.x, cv.y, cv.z, cv.w};
-        float out[4];
-        if (ALPHA1) {
-          const unsigned all = (unsigned)cv.x | ((unsigned)cv.y << 8) | ((unsigned)cv.z << 16) |
-                               ((unsigned)cv.w << 24);
-          // warp-uniform choice: all-fluid neighbourhoods take val / 4
-          if (__all_sync(__activemask(), all == 0x1f1f1f1fu)) {
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-              out[j] = ((((W4[j] + E4[j]) + S4[j]) + N4[j]) + F4[j] * hh * hh) * 0.25f;
-          } else {
-#pragma unroll
-            for (int j = 0; j < 4; j++) out[j] = rb_update1(C4[j], W4[j], E4[j], S4[j], N4[j], F4[j], hh);
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 4; j++)
-            out[j] = rb_update_alpha(C4[j], P4[j], W4[j], E4[j], S4[j], N4[j], F4[j], hh, a.alpha);
-        }
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-          if (!cell_ok(k0 + j, par, gy)) out[j] = P4[j];
-        St::sts4(self + row, make_float4(out[0], out[1], out[2], out[3]));
-      }
+      // parity of this thread's rows: (half + rsub) & 1, rsub's parity is wid & 1
+      if (((half + (wid & 1) + color) & 1) != 0)
+        sweep(std::integral_constant<int, 1>{}, color, half);
+      else
+        sweep(std::integral_constant<int, 0>{}, color, half);
       __syncthreads();
     }
     if (a.zgbc && edge) {
