@@ -237,8 +237,9 @@ using MgArgs = MgArgsT<float>;
 template <int TX, int TY, int HALO>
 struct Tile {
   static constexpr int RX = TX + 2 * HALO, RY = TY + 2 * HALO, HX = RX / 2;
-  // coarse window for the prolongation prologue
-  static constexpr int CW = HX + 2, CH = RY / 2 + 2;
+  // coarse window for the prolongation prologue (rows padded to a multiple
+  // of 4 entries for vector access)
+  static constexpr int CW = HX + 4, CH = RY / 2 + 2;
   static_assert(RX % 4 == 0 && HALO % 4 == 0 && TX % 4 == 0 && TY % 2 == 0, "tile alignment");
   // shared memory for element size ES: p and f in the split layout, codes,
   // the coarse window (values and flags)
@@ -338,6 +339,19 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   }
   __syncthreads();
 
+  // Row mapping of the vectorised phases: a thread handles 4 consecutive
+  // cells of one colour in one row (128-bit shared-memory accesses); G
+  // threads cover a row.  A warp covers R = 32 / G rows two apart and its
+  // partner warp the rows in between, so a row's parity is the same across
+  // a warp and, because a pass covers an even number of rows, fixed for a
+  // thread through a pass: parity-dependent choices are warp-uniform.
+  constexpr int G = HX / 4, R = 32 / G, RPP = NT / G;
+  static_assert(HX % 4 == 0 && NT % G == 0 && 32 % G == 0 && (NT / 32) % 2 == 0,
+                "vector layout");
+  const int lane = tid & 31, wid = tid >> 5;
+  const int k0 = 4 * (lane % G);
+  const int rsub = (wid >> 1) * (2 * R) + (wid & 1) + 2 * (lane / G);
+
   // ---- prologue: correct(p, prolongate(ec)) on the interior cells, with
   // the coarse window staged in shared memory
   if (a.ec) {
@@ -371,38 +385,65 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
       }
     }
     __syncthreads();
+    // prolongate (pressure_solver.cpp:134-172); e * fine flag = e here.
+    // Fine cell (rx, ry) = (2k + par, ry) lies over coarse column k of the
+    // window and coarse row ry / 2; x parity is par and y parity ry & 1, both
+    // fixed across the thread's 4 cells.
 #pragma unroll
     for (int color = 0; color < 2; color++) {
-      for (int ry = ty; ry < RY; ry += NTY) {
-        const int par = (ry + color) & 1;
+      for (int ry = rsub; ry < RY; ry += RPP) {
+        const int par = (ry + color) & 1, yo = ry & 1;
         const int gy = y0 + ry;
         if (gy < 1 || gy >= h - 1) continue;
-        for (int k = tx; k < HX; k += 32) {
-          int rx = 2 * k + par, gx = x0 + rx;
-          int i = (color * RY + ry) * HX + k;
-          if (gx < 1 || gx >= w - 1 || !(sc[i] & C_CENTER)) continue;
-          // prolongate (pressure_solver.cpp:134-172); e * fine flag = e here
-          const S *Es = sec + (ry >> 1) * CW + (rx >> 1);
-          const uint8_t *F = scf + (ry >> 1) * CW + (rx >> 1);
-          auto E = [&](int o) { return St::tof(Es[o]); };
-          bool xo = gx & 1, yo = gy & 1;
-          float ev;
-          if (!xo && !yo) {
-            ev = E(0);
-          } else if (xo && !yo) {
-            const int k = F[0] + F[1];
-            ev = (gx >= w - 2) ? 0.0f : div_rn(E(0) + E(1), a.wsum[k], a.rwsum[k]);
-          } else if (!xo && yo) {
-            const int k = F[0] + F[CW];
-            ev = (gy >= h - 2) ? 0.0f : div_rn(E(0) + E(CW), a.wsum[k], a.rwsum[k]);
-          } else {
-            const int k = F[0] + F[CW + 1] + F[1] + F[CW];
-            ev = (gx >= w - 2 || gy >= h - 2)
-                     ? 0.0f
-                     : div_rn(((E(0) + E(CW + 1)) + E(1)) + E(CW), a.wsum[k], a.rwsum[k]);
-          }
-          sp[i] = St::fromf(St::tof(sp[i]) + ev);
+        const int row = (color * RY + ry) * HX + k0;
+        const unsigned cw4 = *reinterpret_cast<const unsigned *>(sc + row);
+        if ((cw4 & 0x01010101u) == 0u) continue;  // no fluid cell among the 4
+        const int eo = (ry >> 1) * CW + k0;
+        const float4 ea = St::lds4(sec + eo);
+        const float E0[5] = {ea.x, ea.y, ea.z, ea.w, St::tof(sec[eo + 4])};
+        const unsigned fa = *reinterpret_cast<const unsigned *>(scf + eo);
+        const unsigned F0[5] = {fa & 0xffu, (fa >> 8) & 0xffu, (fa >> 16) & 0xffu, fa >> 24,
+                                scf[eo + 4]};
+        float E1[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        unsigned F1[5] = {0u, 0u, 0u, 0u, 0u};
+        if (yo) {
+          const float4 eb = St::lds4(sec + eo + CW);
+          E1[0] = eb.x;
+          E1[1] = eb.y;
+          E1[2] = eb.z;
+          E1[3] = eb.w;
+          E1[4] = St::tof(sec[eo + CW + 4]);
+          const unsigned fb = *reinterpret_cast<const unsigned *>(scf + eo + CW);
+          F1[0] = fb & 0xffu;
+          F1[1] = (fb >> 8) & 0xffu;
+          F1[2] = (fb >> 16) & 0xffu;
+          F1[3] = fb >> 24;
+          F1[4] = scf[eo + CW + 4];
         }
+        const float4 pv = St::lds4(sp + row);
+        float out[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int gx = x0 + 2 * (k0 + j) + par;
+          if (gx < 1 || gx >= w - 1 || !((cw4 >> (8 * j)) & C_CENTER)) continue;
+          float pe;
+          if (!par && !yo) {
+            pe = E0[j];
+          } else if (par && !yo) {
+            const int k = F0[j] + F0[j + 1];
+            pe = (gx >= w - 2) ? 0.0f : div_rn(E0[j] + E0[j + 1], a.wsum[k], a.rwsum[k]);
+          } else if (!par && yo) {
+            const int k = F0[j] + F1[j];
+            pe = (gy >= h - 2) ? 0.0f : div_rn(E0[j] + E1[j], a.wsum[k], a.rwsum[k]);
+          } else {
+            const int k = F0[j] + F1[j + 1] + F0[j + 1] + F1[j];
+            pe = (gx >= w - 2 || gy >= h - 2)
+                     ? 0.0f
+                     : div_rn(((E0[j] + E1[j + 1]) + E0[j + 1]) + E1[j], a.wsum[k], a.rwsum[k]);
+          }
+          out[j] = out[j] + pe;
+        }
+        St::sts4(sp + row, make_float4(out[0], out[1], out[2], out[3]));
       }
     }
     __syncthreads();
@@ -435,18 +476,8 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
     __syncthreads();
   }
 
-  // ---- red-black sweeps: a thread updates 4 consecutive cells of one colour
-  // in one row (128-bit shared-memory accesses); G threads cover a row.  A
-  // warp covers R = 32 / G rows two apart and its partner warp the rows in
-  // between, so a row's parity is the same across a warp and, because a
-  // pass covers an even number of rows, fixed for a thread through a half
-  // sweep: the parity-dependent selects become two specialised loops.
-  constexpr int G = HX / 4, R = 32 / G, RPP = NT / G;
-  static_assert(HX % 4 == 0 && NT % G == 0 && 32 % G == 0 && (NT / 32) % 2 == 0,
-                "vector layout");
-  const int lane = tid & 31, wid = tid >> 5;
-  const int k0 = 4 * (lane % G);
-  const int rsub = (wid >> 1) * (2 * R) + (wid & 1) + 2 * (lane / G);
+  // ---- red-black sweeps: a thread updates the 4 cells of its row group
+  // (see the row mapping above)
   const float hh = a.hh;
   const bool inner = x0 >= 1 && y0 >= 1 && x0 + RX <= w - 1 && y0 + RY <= h - 1;
   // which of the thread's 4 cells may be smoothed, per row parity: k >= 1 -
