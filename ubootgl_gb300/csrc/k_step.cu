@@ -138,9 +138,9 @@ __device__ __forceinline__ void k_vbc_body(VelBufs v, int fx, int fy, Bcs bc, in
   int nx = (H - 2) + (W - 1);
   float m = 0.0f;
   if (t < nx) {
-    if (do_vx) vbc_component<true>(v.vx[fx], v.vx[0], v.vx[1], v.pitch, W - 1, H, bc, t, m);
+    if (do_vx) vbc_component<true>(pick(v.vx, fx), v.vx[0], v.vx[1], v.pitch, W - 1, H, bc, t, m);
   } else if (do_vy) {
-    vbc_component<false>(v.vy[fy], v.vy[0], v.vy[1], v.pitch, W, H - 1, bc, t - nx, m);
+    vbc_component<false>(pick(v.vy, fy), v.vy[0], v.vy[1], v.pitch, W, H - 1, bc, t - nx, m);
   }
   // max |boundary value| for the next step's CFL dt (interior faces come
   // from the gradient kernel)
@@ -262,7 +262,7 @@ __device__ __forceinline__ void k_diffuse_body(VelBufs v, int srcx, int srcy,
   if (bz == 0) {
     // vx: interior faces x in [1, W-3], y in [1, H-2]
     if (!(comps & 1) || y < 1 || y >= H - 1 || x > W - 3 || x + 3 < 1) return;
-    const float *s = v.vx[srcx];
+    const float *s = pick(v.vx, srcx);
     float4 C = ld4(s, P, x, y), N = ld4(s, P, x, y + 1), S = ld4(s, P, x, y - 1);
     uchar4 K = __ldg(reinterpret_cast<const uchar4 *>(v.cx + (size_t)y * P + x));
     float L = x >= 1 ? ld(s, P, x - 1, y) : 0.0f;
@@ -280,11 +280,11 @@ __device__ __forceinline__ void k_diffuse_body(VelBufs v, int srcx, int srcy,
       val = val + ((k & FC_T4) ? comp(S, j) : -c);
       o[j] = (k & FC_M) ? div_rn(c + a * val, den, rden) : 0.0f;
     }
-    st4_masked(v.vx[1 - srcx] + (size_t)y * P, x, 1, W - 3, o);
+    st4_masked(pick(v.vx, 1 - srcx) + (size_t)y * P, x, 1, W - 3, o);
   } else {
     // vy: interior faces x in [1, W-2], y in [1, H-3]
     if (!(comps & 2) || y < 1 || y >= H - 2 || x > W - 2 || x + 3 < 1) return;
-    const float *s = v.vy[srcy];
+    const float *s = pick(v.vy, srcy);
     float4 C = ld4(s, P, x, y), N = ld4(s, P, x, y + 1), S = ld4(s, P, x, y - 1);
     uchar4 K = __ldg(reinterpret_cast<const uchar4 *>(v.cy + (size_t)y * P + x));
     float L = x >= 1 ? ld(s, P, x - 1, y) : 0.0f;
@@ -302,7 +302,7 @@ __device__ __forceinline__ void k_diffuse_body(VelBufs v, int srcx, int srcy,
       val = val + ((k & FC_T4) ? t4 : -c);
       o[j] = (k & FC_M) ? div_rn(c + a * val, den, rden) : 0.0f;
     }
-    st4_masked(v.vy[1 - srcy] + (size_t)y * P, x, 1, W - 2, o);
+    st4_masked(pick(v.vy, 1 - srcy) + (size_t)y * P, x, 1, W - 2, o);
   }
 }
 __global__ void __launch_bounds__(256) k_diffuse(VelBufs v, int srcx, int srcy,
@@ -408,8 +408,8 @@ __device__ __forceinline__ void k_advect_body(VelBufs v, int srcx, int srcy,
   __shared__ float syv[AD_SH * AD_SW];
   __shared__ uint8_t scx[AD_TY * AD_TX], scy[AD_TY * AD_TX];
   const int W = v.W, H = v.H, P = v.pitch;
-  const float *vx = v.vx[srcx];
-  const float *vy = v.vy[srcy];
+  const float *vx = pick(v.vx, srcx);
+  const float *vy = pick(v.vy, srcy);
   const int X0 = bx * AD_TX, Y0 = by * AD_TY;
   const int sx0 = X0 - AD_H, sy0 = Y0 - AD_H;
   const int tid = threadIdx.y * BX + threadIdx.x;
@@ -440,7 +440,7 @@ __device__ __forceinline__ void k_advect_body(VelBufs v, int srcx, int srcy,
   const float chalf = sc->chalf, cfull = sc->cfull;
   auto SX = [&](int x, int y) { return sxv[(y - sy0) * AD_SW + (x - sx0)]; };
   auto SY = [&](int x, int y) { return syv[(y - sy0) * AD_SW + (x - sx0)]; };
-  float *outx = v.vx[1 - srcx], *outy = v.vy[1 - srcy];
+  float *outx = pick(v.vx, 1 - srcx), *outy = pick(v.vy, 1 - srcy);
   for (int i = tid; i < AD_TX * AD_TY; i += 256) {
     int ty = i / AD_TX, tx = i - ty * AD_TX;
     int x = X0 + tx, y = Y0 + ty;
@@ -569,7 +569,7 @@ __device__ __forceinline__ void k_gradient_body(VelBufs v, int fx, int fy,
   float m = 0.0f;
   if (y >= 1 && y < H - 1 && x <= W - 2 && x + 3 >= 1) {
     const float ih = sc->ih;
-    float *vx = v.vx[fx], *vy = v.vy[fy];
+    float *vx = pick(v.vx, fx), *vy = pick(v.vy, fy);
     float4 P0 = ld4(p, P, x, y), PN = ld4(p, P, x, y + 1);
     float PR = x + 4 < W ? ld(p, P, x + 4, y) : 0.0f;
     float4 U = *reinterpret_cast<const float4 *>(vx + (size_t)y * P + x);

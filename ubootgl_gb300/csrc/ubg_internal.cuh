@@ -106,6 +106,10 @@ struct VelBufs {
   const uint8_t *cx, *cy;
 };
 constexpr unsigned FC_M = 1, FC_T1 = 2, FC_T2 = 4, FC_T3 = 8, FC_T4 = 16, FC_A = 32;
+// Buffer f of a pair, chosen without indexing the array: a run-time index
+// into a kernel parameter's array makes the compiler copy the parameter to
+// local memory.
+__device__ __forceinline__ float *pick(float *const (&b)[2], int f) { return f ? b[1] : b[0]; }
 // Builds the face codes from the cell flags.
 void launch_face_codes(const VelBufs &v, const uint8_t *flag, uint8_t *cx, uint8_t *cy,
                        cudaStream_t st);
