@@ -340,17 +340,27 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   __syncthreads();
 
   // Row mapping of the vectorised phases: a thread handles 4 consecutive
-  // cells of one colour in one row (128-bit shared-memory accesses); G
-  // threads cover a row.  A warp covers R = 32 / G rows two apart and its
-  // partner warp the rows in between, so a row's parity is the same across
-  // a warp and, because a pass covers an even number of rows, fixed for a
-  // thread through a pass: parity-dependent choices are warp-uniform.
-  constexpr int G = HX / 4, R = 32 / G, RPP = NT / G;
-  static_assert(HX % 4 == 0 && NT % G == 0 && 32 % G == 0 && (NT / 32) % 2 == 0,
-                "vector layout");
+  // cells of one colour in one row (128-bit shared-memory accesses).  A
+  // warp covers 32 entries (k) of 4 rows two apart, 8 lanes per row (each
+  // quarter-warp one row: no bank conflicts); its partner warp takes the
+  // rows in between.  So a row's parity is the same across a warp and,
+  // because a pass covers an even number of rows, fixed for a thread
+  // through a pass: parity-dependent choices are warp-uniform.  The compact
+  // 4-row footprint also keeps fewer warps straddling obstacle edges (at
+  // 4096x2048 with 12 discs: 9 % of warp passes instead of 16 % for 2 rows
+  // of 64 entries).
+  constexpr int KH = HX / 32, RPP = NT / (HX / 4);
+  static_assert(HX % 32 == 0 && (NT / 32) % (2 * KH) == 0, "vector layout");
   const int lane = tid & 31, wid = tid >> 5;
-  const int k0 = 4 * (lane % G);
-  const int rsub = (wid >> 1) * (2 * R) + (wid & 1) + 2 * (lane / G);
+  const int kh = wid % KH, wpar = (wid / KH) & 1;
+  const int k0 = 4 * ((lane & 7) + 8 * kh);
+  const int rsub = (wid / (2 * KH)) * 8 + wpar + 2 * (lane >> 3);
+  // The prolongation prologue measures faster with wide rows: G threads per
+  // row, a warp on 32 / G rows two apart, its partner warp between them.
+  constexpr int G = HX / 4, RW = 32 / G;
+  static_assert(NT % G == 0 && 32 % G == 0, "vector layout");
+  const int k0w = 4 * (lane % G);
+  const int rsubw = (wid >> 1) * (2 * RW) + (wid & 1) + 2 * (lane / G);
 
   // ---- prologue: correct(p, prolongate(ec)) on the interior cells, with
   // the coarse window staged in shared memory
@@ -391,14 +401,14 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
     // fixed across the thread's 4 cells.
 #pragma unroll
     for (int color = 0; color < 2; color++) {
-      for (int ry = rsub; ry < RY; ry += RPP) {
+      for (int ry = rsubw; ry < RY; ry += RPP) {
         const int par = (ry + color) & 1, yo = ry & 1;
         const int gy = y0 + ry;
         if (gy < 1 || gy >= h - 1) continue;
-        const int row = (color * RY + ry) * HX + k0;
+        const int row = (color * RY + ry) * HX + k0w;
         const unsigned cw4 = *reinterpret_cast<const unsigned *>(sc + row);
         if ((cw4 & 0x01010101u) == 0u) continue;  // no fluid cell among the 4
-        const int eo = (ry >> 1) * CW + k0;
+        const int eo = (ry >> 1) * CW + k0w;
         const float4 ea = St::lds4(sec + eo);
         const float E0[5] = {ea.x, ea.y, ea.z, ea.w, St::tof(sec[eo + 4])};
         const unsigned fa = *reinterpret_cast<const unsigned *>(scf + eo);
@@ -424,7 +434,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
         float out[4] = {pv.x, pv.y, pv.z, pv.w};
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          const int gx = x0 + 2 * (k0 + j) + par;
+          const int gx = x0 + 2 * (k0w + j) + par;
           if (gx < 1 || gx >= w - 1 || !((cw4 >> (8 * j)) & C_CENTER)) continue;
           float pe;
           if (!par && !yo) {
@@ -520,11 +530,16 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
       const float F4[4] = {fv.x, fv.y, fv.z, fv.w};
       float out[4];
       if (ALPHA1) {
-        // warp-uniform choice: all-fluid neighbourhoods take val / 4
-        if (__all_sync(__activemask(), cw == 0x1f1f1f1fu)) {
+        // all-fluid neighbourhoods take val / 4, and cells that are all
+        // solid (inside obstacles, outside the domain) are 0 (a per-thread
+        // choice: a warp vote here cost more than the divergence it saves)
+        if (cw == 0x1f1f1f1fu) {
 #pragma unroll
           for (int j = 0; j < 4; j++)
             out[j] = ((((W4[j] + E4[j]) + S4[j]) + N4[j]) + F4[j] * hh * hh) * 0.25f;
+        } else if ((cw & 0x01010101u) == 0u) {
+#pragma unroll
+          for (int j = 0; j < 4; j++) out[j] = 0.0f;
         } else {
 #pragma unroll
           for (int j = 0; j < 4; j++)
@@ -554,8 +569,8 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
 #pragma unroll
     for (int color = 1; color >= 0; color--) {
       half++;
-      // parity of this thread's rows: (half + rsub) & 1, rsub's parity is wid & 1
-      if (((half + (wid & 1) + color) & 1) != 0)
+      // parity of this thread's rows: (half + rsub) & 1, rsub's parity is wpar
+      if (((half + wpar + color) & 1) != 0)
         sweep(std::integral_constant<int, 1>{}, color, half);
       else
         sweep(std::integral_constant<int, 0>{}, color, half);
