@@ -664,20 +664,73 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   // ---- restrict (pressure_solver.cpp:118-132) onto the coarse tile -------
   if (a.rc) {
     const int cx0 = bx * (TX / 2), cy0 = by * (TY / 2);
-    for (int q = tid; q < (TX / 2) * (TY / 2); q += NT) {
-      int cyy = q / (TX / 2), cxx = q - cyy * (TX / 2);
-      int X = cx0 + cxx, Y = cy0 + cyy;
-      if (X >= a.cw || Y >= a.ch) continue;
-      float v = 0.0f;
-      if (X >= 1 && X < a.cw - 1 && Y >= 1 && Y < a.ch - 1) {
-        int rx = 2 * X - x0, ry = 2 * Y - y0;
-        auto R = [&](int dx, int dy) { return St::tof(sf[IDX(rx + dx, ry + dy)]); };
-        v = (R(-1, -1) * 1.0f + R(0, -1) * 2.0f) + R(1, -1) * 1.0f;
-        v = v + ((R(-1, 0) * 2.0f + R(0, 0) * 4.0f) + R(1, 0) * 2.0f);
-        v = v + ((R(-1, 1) * 1.0f + R(0, 1) * 2.0f) + R(1, 1) * 1.0f);
-        v = v * a.rfac;
+    // one coarse cell: full weighting of the 3x3 fine residuals around it
+    auto restrict1 = [&](float m1, float c0, float p1, float m2, float c2, float p2, float m3,
+                         float c3, float p3) {
+      float v = (m1 * 1.0f + c0 * 2.0f) + p1 * 1.0f;
+      v = v + ((m2 * 2.0f + c2 * 4.0f) + p2 * 2.0f);
+      v = v + ((m3 * 1.0f + c3 * 2.0f) + p3 * 1.0f);
+      return v * a.rfac;
+    };
+    if constexpr (HALO % 8 == 0 && (TX / 2) % 4 == 0) {
+      // 4 consecutive coarse cells per thread.  Coarse column X sits over
+      // fine column rx = 2X - x0 (even): its centre values are entries kc =
+      // rx / 2 of the colour-(ry & 1) rows, its west / east neighbours
+      // entries kc - 1 / kc of the other colour; kc is a multiple of 4.
+      constexpr int CXG = TX / 8, NQR = CXG * (TY / 2);
+      for (int q = tid; q < NQR; q += NT) {
+        const int cyy = q / CXG, g = q - cyy * CXG;
+        const int X0 = cx0 + 4 * g, Y = cy0 + cyy;
+        if (X0 >= a.cw || Y >= a.ch) continue;
+        const int ry = 2 * Y - y0, kc = (2 * X0 - x0) >> 1;
+        float cen[3][4], oth[3][5];
+#pragma unroll
+        for (int e = 0; e < 3; e++) {
+          const int r = ry + e - 1, c = r & 1;
+          const float4 u = St::lds4(sf + (c * RY + r) * HX + kc);
+          const float4 o = St::lds4(sf + ((c ^ 1) * RY + r) * HX + kc);
+          cen[e][0] = u.x;
+          cen[e][1] = u.y;
+          cen[e][2] = u.z;
+          cen[e][3] = u.w;
+          oth[e][0] = St::tof(sf[((c ^ 1) * RY + r) * HX + kc - 1]);
+          oth[e][1] = o.x;
+          oth[e][2] = o.y;
+          oth[e][3] = o.z;
+          oth[e][4] = o.w;
+        }
+        float v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int X = X0 + j;
+          v[j] = 0.0f;
+          if (X >= 1 && X < a.cw - 1 && Y >= 1 && Y < a.ch - 1)
+            v[j] = restrict1(oth[0][j], cen[0][j], oth[0][j + 1], oth[1][j], cen[1][j],
+                             oth[1][j + 1], oth[2][j], cen[2][j], oth[2][j + 1]);
+        }
+        S *dst = a.rc + (size_t)Y * a.cpitch + X0;
+        if (X0 + 3 < a.cw) {
+          St::st4(dst, make_float4(v[0], v[1], v[2], v[3]));
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            if (X0 + j < a.cw) dst[j] = St::fromf(v[j]);
+        }
       }
-      a.rc[(size_t)Y * a.cpitch + X] = St::fromf(v);
+    } else {
+      for (int q = tid; q < (TX / 2) * (TY / 2); q += NT) {
+        int cyy = q / (TX / 2), cxx = q - cyy * (TX / 2);
+        int X = cx0 + cxx, Y = cy0 + cyy;
+        if (X >= a.cw || Y >= a.ch) continue;
+        float v = 0.0f;
+        if (X >= 1 && X < a.cw - 1 && Y >= 1 && Y < a.ch - 1) {
+          int rx = 2 * X - x0, ry = 2 * Y - y0;
+          auto R = [&](int dx, int dy) { return St::tof(sf[IDX(rx + dx, ry + dy)]); };
+          v = restrict1(R(-1, -1), R(0, -1), R(1, -1), R(-1, 0), R(0, 0), R(1, 0), R(-1, 1),
+                        R(0, 1), R(1, 1));
+        }
+        a.rc[(size_t)Y * a.cpitch + X] = St::fromf(v);
+      }
     }
   }
 }
@@ -1013,9 +1066,10 @@ void set_multi_attr() {
                                 cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 }
 
-void init_kernel_attributes() {
-  static bool done = false;
-  if (done) return;
+// Sets the shared-memory attributes of every smoother and tail kernel, once
+// per process (function-local static initialisation is thread-safe; the
+// server's worker thread and the caller's threads may race here).
+static void set_all_kernel_attributes() {
   set_multi_attr<112, 50, 8>();
   set_multi_attr<48, 16, 8>();
   set_multi_attr<40, 8, 12>();
@@ -1032,7 +1086,11 @@ void init_kernel_attributes() {
   set_vcycle_attrs<__nv_bfloat16>();
   set_tail_attr<__half, double>();
   set_tail_attr<__nv_bfloat16, double>();
-  done = true;
+}
+
+void init_kernel_attributes() {
+  static const bool done = (set_all_kernel_attributes(), true);
+  (void)done;
 }
 
 // 3 sweeps with an optional restriction epilogue need HALO >= 8; the tile
