@@ -272,69 +272,86 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   const int x0 = bx * TX - HALO, y0 = by * TY - HALO;
   const int w = a.w, h = a.h, P = a.pitch;
 
-  // ---- load p, f, code (float4 / uchar4 per thread; x0 is a multiple of 4).
+  // ---- load p, f, code: 8 consecutive cells per thread and item (two
+  // float4 / two uchar4 loads; x0 is a multiple of 4), stored as 4 cells of
+  // each colour (one 128-bit store per colour, codes one 32-bit store).
   // One array at a time, all of a thread's loads of that array in flight
   // together, into the red/black-split layout.
-  constexpr int NQ = RY * (RX / 4), NIT = (NQ + NT - 1) / NT;
+  static_assert(RX % 8 == 0, "8-cell load groups");
+  constexpr int NQ = RY * (RX / 8), NIT = (NQ + NT - 1) / NT;
   auto load_split = [&](const S *src, S *dst, bool zero) {
-    float4 v[NIT];
+    float4 v[NIT][2];
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
-      int q = tid + it * NT;
-      int ry = q / (RX / 4), g = q - ry * (RX / 4);
-      int gx = x0 + 4 * g, gy = y0 + ry;
-      v[it] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (!zero && q < NQ && gy >= 0 && gy < h && gx >= 0 && gx < w)
-        v[it] = St::ldg4(src + (size_t)gy * P + gx);
+      const int q = tid + it * NT;
+      const int ry = q / (RX / 8), g = q - ry * (RX / 8);
+      const int gx = x0 + 8 * g, gy = y0 + ry;
+      const bool row = !zero && q < NQ && gy >= 0 && gy < h;
+#pragma unroll
+      for (int hf = 0; hf < 2; hf++) {
+        const int x = gx + 4 * hf;
+        v[it][hf] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (row && x >= 0 && x < w) v[it][hf] = St::ldg4(src + (size_t)gy * P + x);
+      }
     }
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
-      int q = tid + it * NT;
+      const int q = tid + it * NT;
       if (q >= NQ) break;
-      int ry = q / (RX / 4), g = q - ry * (RX / 4);
-      int gx = x0 + 4 * g;
-      float4 p4 = v[it];
-      if (gx + 3 >= w) {
-        if (gx + 1 >= w) p4.y = 0.f;
-        if (gx + 2 >= w) p4.z = 0.f;
-        p4.w = 0.f;
+      const int ry = q / (RX / 8), g = q - ry * (RX / 8);
+      const int gx = x0 + 8 * g;
+      float c[8] = {v[it][0].x, v[it][0].y, v[it][0].z, v[it][0].w,
+                    v[it][1].x, v[it][1].y, v[it][1].z, v[it][1].w};
+      if (gx + 7 >= w) {  // cells at and beyond the grid's width are 0
+#pragma unroll
+        for (int i = 1; i < 8; i++)
+          if (gx + i >= w) c[i] = 0.f;
       }
-      int c0 = ry & 1;
-      St::sts2(dst + (c0 * RY + ry) * HX + 2 * g, p4.x, p4.z);
-      St::sts2(dst + ((c0 ^ 1) * RY + ry) * HX + 2 * g, p4.y, p4.w);
+      const int c0 = ry & 1;
+      St::sts4(dst + (c0 * RY + ry) * HX + 4 * g, make_float4(c[0], c[2], c[4], c[6]));
+      St::sts4(dst + ((c0 ^ 1) * RY + ry) * HX + 4 * g, make_float4(c[1], c[3], c[5], c[7]));
     }
   };
   load_split(a.in, sp, a.zero_init != 0);
   load_split(a.rhs, sf, false);
   {
-    uchar4 cv[NIT];
+    unsigned cv[NIT][2];
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
-      int q = tid + it * NT;
-      int ry = q / (RX / 4), g = q - ry * (RX / 4);
-      int gx = x0 + 4 * g, gy = y0 + ry;
-      cv[it] = make_uchar4(0, 0, 0, 0);
-      if (q < NQ && gy >= 0 && gy < h && gx >= 0 && gx < w)
-        cv[it] = __ldg(reinterpret_cast<const uchar4 *>(a.code + (size_t)gy * P + gx));
+      const int q = tid + it * NT;
+      const int ry = q / (RX / 8), g = q - ry * (RX / 8);
+      const int gx = x0 + 8 * g, gy = y0 + ry;
+      const bool row = q < NQ && gy >= 0 && gy < h;
+#pragma unroll
+      for (int hf = 0; hf < 2; hf++) {
+        const int x = gx + 4 * hf;
+        cv[it][hf] = 0u;
+        if (row && x >= 0 && x < w)
+          cv[it][hf] = __ldg(reinterpret_cast<const unsigned *>(a.code + (size_t)gy * P + x));
+      }
     }
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
-      int q = tid + it * NT;
+      const int q = tid + it * NT;
       if (q >= NQ) break;
-      int ry = q / (RX / 4), g = q - ry * (RX / 4);
-      int gx = x0 + 4 * g;
-      uchar4 c4 = cv[it];
-      if (gx + 3 >= w) {
-        if (gx + 1 >= w) c4.y = 0;
-        if (gx + 2 >= w) c4.z = 0;
-        c4.w = 0;
+      const int ry = q / (RX / 8), g = q - ry * (RX / 8);
+      const int gx = x0 + 8 * g;
+      unsigned lo = cv[it][0], hi = cv[it][1];
+      if (gx + 7 >= w) {  // byte i of (lo, hi) is cell gx + i
+#pragma unroll
+        for (int i = 1; i < 8; i++)
+          if (gx + i >= w) {
+            if (i < 4)
+              lo &= ~(0xffu << (8 * i));
+            else
+              hi &= ~(0xffu << (8 * (i - 4)));
+          }
       }
-      int c0 = ry & 1;
-      int base0 = (c0 * RY + ry) * HX + 2 * g, base1 = ((c0 ^ 1) * RY + ry) * HX + 2 * g;
-      sc[base0] = c4.x;
-      sc[base0 + 1] = c4.z;
-      sc[base1] = c4.y;
-      sc[base1 + 1] = c4.w;
+      // even bytes to the row's colour, odd bytes to the other one
+      const unsigned ev = __byte_perm(lo, hi, 0x6420), od = __byte_perm(lo, hi, 0x7531);
+      const int c0 = ry & 1;
+      *reinterpret_cast<unsigned *>(sc + (c0 * RY + ry) * HX + 4 * g) = ev;
+      *reinterpret_cast<unsigned *>(sc + ((c0 ^ 1) * RY + ry) * HX + 4 * g) = od;
     }
   }
   __syncthreads();
