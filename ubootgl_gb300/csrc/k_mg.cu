@@ -330,6 +330,74 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
           cv[it][hf] = __ldg(reinterpret_cast<const unsigned *>(a.code + (size_t)gy * P + x));
       }
     }
+    // coarse window of the prolongation prologue (post-smoothing): loaded
+    // while the code loads are in flight, stored before the same barrier
+    if (a.ec) {
+      constexpr int CW = T::CW, CH = T::CH;
+      S *sec = reinterpret_cast<S *>(sc + 2 * RY * HX);
+      uint8_t *scf = reinterpret_cast<uint8_t *>(sc + 2 * RY * HX) +
+                     ((size_t)CW * CH * sizeof(S) + 15) / 16 * 16;
+      const int cxa = x0 >> 1, cya = y0 >> 1;
+      // all of a thread's loads in flight together, then the stores
+      if constexpr (HALO % 8 == 0) {
+        // cxa is a multiple of 4: 4 coarse entries per load (value and flag)
+        constexpr int CQ4 = (CW / 4) * CH, CIT = (CQ4 + NT - 1) / NT;
+        static_assert(CW % 4 == 0, "window rows of whole vectors");
+        float4 ev[CIT];
+        unsigned fv[CIT];
+  #pragma unroll
+        for (int it = 0; it < CIT; it++) {
+          const int q = tid + it * NT;
+          const int ly = q / (CW / 4), lx = 4 * (q - ly * (CW / 4));
+          const int cx = cxa + lx, cy = cya + ly;
+          ev[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+          fv[it] = 0u;
+          if (q < CQ4 && cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
+            ev[it] = St::ldg4(a.ec + (size_t)cy * a.cpitch + cx);
+            fv[it] = __ldg(reinterpret_cast<const unsigned *>(a.codec + (size_t)cy * a.cpitch + cx)) &
+                     0x01010101u;
+            if (cx + 3 >= a.cw) {  // entries at and beyond the level's width are 0
+              if (cx + 1 >= a.cw) ev[it].y = 0.f, fv[it] &= 0x000000ffu;
+              if (cx + 2 >= a.cw) ev[it].z = 0.f, fv[it] &= 0x0000ffffu;
+              ev[it].w = 0.f;
+              fv[it] &= 0x00ffffffu;
+            }
+          }
+        }
+  #pragma unroll
+        for (int it = 0; it < CIT; it++) {
+          const int q = tid + it * NT;
+          if (q < CQ4) {
+            St::sts4(sec + 4 * q, ev[it]);
+            *reinterpret_cast<unsigned *>(scf + 4 * q) = fv[it];
+          }
+        }
+      } else {
+        constexpr int CQ = CW * CH, CIT = (CQ + NT - 1) / NT;
+        float ev[CIT];
+        uint8_t fv[CIT];
+  #pragma unroll
+        for (int it = 0; it < CIT; it++) {
+          int q = tid + it * NT;
+          int ly = q / CW, lx = q - ly * CW;
+          int cx = cxa + lx, cy = cya + ly;
+          ev[it] = 0.0f;
+          fv[it] = 0;
+          if (q < CQ && cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
+            ev[it] = St::ldg1(a.ec + (size_t)cy * a.cpitch + cx);
+            fv[it] = __ldg(a.codec + (size_t)cy * a.cpitch + cx) & 1u;
+          }
+        }
+  #pragma unroll
+        for (int it = 0; it < CIT; it++) {
+          int q = tid + it * NT;
+          if (q < CQ) {
+            sec[q] = St::fromf(ev[it]);
+            scf[q] = fv[it];
+          }
+        }
+      }
+    }
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
       const int q = tid + it * NT;
@@ -379,74 +447,13 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   const int k0w = 4 * (lane % G);
   const int rsubw = (wid >> 1) * (2 * RW) + (wid & 1) + 2 * (lane / G);
 
-  // ---- prologue: correct(p, prolongate(ec)) on the interior cells, with
-  // the coarse window staged in shared memory
+  // ---- prologue: correct(p, prolongate(ec)) on the interior cells, from
+  // the coarse window staged with the field loads above
   if (a.ec) {
     constexpr int CW = T::CW, CH = T::CH;
     S *sec = reinterpret_cast<S *>(sc + 2 * RY * HX);
     uint8_t *scf = reinterpret_cast<uint8_t *>(sc + 2 * RY * HX) +
                    ((size_t)CW * CH * sizeof(S) + 15) / 16 * 16;
-    const int cxa = x0 >> 1, cya = y0 >> 1;
-    // all of a thread's loads in flight together, then the stores
-    if constexpr (HALO % 8 == 0) {
-      // cxa is a multiple of 4: 4 coarse entries per load (value and flag)
-      constexpr int CQ4 = (CW / 4) * CH, CIT = (CQ4 + NT - 1) / NT;
-      static_assert(CW % 4 == 0, "window rows of whole vectors");
-      float4 ev[CIT];
-      unsigned fv[CIT];
-#pragma unroll
-      for (int it = 0; it < CIT; it++) {
-        const int q = tid + it * NT;
-        const int ly = q / (CW / 4), lx = 4 * (q - ly * (CW / 4));
-        const int cx = cxa + lx, cy = cya + ly;
-        ev[it] = make_float4(0.f, 0.f, 0.f, 0.f);
-        fv[it] = 0u;
-        if (q < CQ4 && cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
-          ev[it] = St::ldg4(a.ec + (size_t)cy * a.cpitch + cx);
-          fv[it] = __ldg(reinterpret_cast<const unsigned *>(a.codec + (size_t)cy * a.cpitch + cx)) &
-                   0x01010101u;
-          if (cx + 3 >= a.cw) {  // entries at and beyond the level's width are 0
-            if (cx + 1 >= a.cw) ev[it].y = 0.f, fv[it] &= 0x000000ffu;
-            if (cx + 2 >= a.cw) ev[it].z = 0.f, fv[it] &= 0x0000ffffu;
-            ev[it].w = 0.f;
-            fv[it] &= 0x00ffffffu;
-          }
-        }
-      }
-#pragma unroll
-      for (int it = 0; it < CIT; it++) {
-        const int q = tid + it * NT;
-        if (q < CQ4) {
-          St::sts4(sec + 4 * q, ev[it]);
-          *reinterpret_cast<unsigned *>(scf + 4 * q) = fv[it];
-        }
-      }
-    } else {
-      constexpr int CQ = CW * CH, CIT = (CQ + NT - 1) / NT;
-      float ev[CIT];
-      uint8_t fv[CIT];
-#pragma unroll
-      for (int it = 0; it < CIT; it++) {
-        int q = tid + it * NT;
-        int ly = q / CW, lx = q - ly * CW;
-        int cx = cxa + lx, cy = cya + ly;
-        ev[it] = 0.0f;
-        fv[it] = 0;
-        if (q < CQ && cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
-          ev[it] = St::ldg1(a.ec + (size_t)cy * a.cpitch + cx);
-          fv[it] = __ldg(a.codec + (size_t)cy * a.cpitch + cx) & 1u;
-        }
-      }
-#pragma unroll
-      for (int it = 0; it < CIT; it++) {
-        int q = tid + it * NT;
-        if (q < CQ) {
-          sec[q] = St::fromf(ev[it]);
-          scf[q] = fv[it];
-        }
-      }
-    }
-    __syncthreads();
     // prolongate (pressure_solver.cpp:134-172); e * fine flag = e here.
     // Fine cell (rx, ry) = (2k + par, ry) lies over coarse column k of the
     // window and coarse row ry / 2; x parity is par and y parity ry & 1, both
