@@ -279,8 +279,8 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   // together, into the red/black-split layout.
   static_assert(RX % 8 == 0, "8-cell load groups");
   constexpr int NQ = RY * (RX / 8), NIT = (NQ + NT - 1) / NT;
-  auto load_split = [&](const S *src, S *dst, bool zero) {
-    float4 v[NIT][2];
+  using Items = float4[NIT][2];
+  auto load_issue = [&](const S *src, bool zero, Items &v) {
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
       const int q = tid + it * NT;
@@ -294,6 +294,8 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
         if (row && x >= 0 && x < w) v[it][hf] = St::ldg4(src + (size_t)gy * P + x);
       }
     }
+  };
+  auto load_store = [&](S *dst, const Items &v) {
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
       const int q = tid + it * NT;
@@ -312,9 +314,15 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
       St::sts4(dst + ((c0 ^ 1) * RY + ry) * HX + 4 * g, make_float4(c[1], c[3], c[5], c[7]));
     }
   };
-  load_split(a.in, sp, a.zero_init != 0);
-  load_split(a.rhs, sf, false);
   {
+    Items vp;
+    load_issue(a.in, a.zero_init != 0, vp);
+    load_store(sp, vp);
+  }
+  {
+    // f, the codes and the coarse window: all loads in flight together
+    Items vf;
+    load_issue(a.rhs, false, vf);
     unsigned cv[NIT][2];
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
@@ -398,6 +406,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
         }
       }
     }
+    load_store(sf, vf);
 #pragma unroll
     for (int it = 0; it < NIT; it++) {
       const int q = tid + it * NT;
