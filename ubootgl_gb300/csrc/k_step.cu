@@ -404,36 +404,50 @@ constexpr int AD_SW = AD_TX + 2 * AD_H, AD_SH = AD_TY + 2 * AD_H;
 
 __device__ __forceinline__ void k_advect_body(VelBufs v, int srcx, int srcy,
                                                 const StepScalars *__restrict__ sc, const int bx, const int by, const int bz) {
-  __shared__ float sxv[AD_SH * AD_SW];
-  __shared__ float syv[AD_SH * AD_SW];
-  __shared__ uint8_t scx[AD_TY * AD_TX], scy[AD_TY * AD_TX];
+  __shared__ __align__(16) float sxv[AD_SH * AD_SW];
+  __shared__ __align__(16) float syv[AD_SH * AD_SW];
+  __shared__ __align__(16) uint8_t scx[AD_TY * AD_TX], scy[AD_TY * AD_TX];
   const int W = v.W, H = v.H, P = v.pitch;
   const float *vx = pick(v.vx, srcx);
   const float *vy = pick(v.vy, srcy);
   const int X0 = bx * AD_TX, Y0 = by * AD_TY;
   const int sx0 = X0 - AD_H, sy0 = Y0 - AD_H;
   const int tid = threadIdx.y * BX + threadIdx.x;
-  for (int i = tid; i < AD_SH * AD_SW; i += 256) {
-    int ry = i / AD_SW, rx = i - ry * AD_SW;
-    int gx = sx0 + rx, gy = sy0 + ry;
-    float a = 0.0f, b = 0.0f;
+  // staging: 4 entries per load (sx0 and X0 are multiples of 4, so every
+  // float4 / uchar4 lies inside its row's pitch); entries outside a
+  // component's extent are 0
+  static_assert(AD_SW % 4 == 0 && AD_H % 4 == 0 && AD_TX % 4 == 0, "vector staging");
+  for (int i = tid; i < AD_SH * (AD_SW / 4); i += 256) {
+    const int ry = i / (AD_SW / 4), rx = 4 * (i - ry * (AD_SW / 4));
+    const int gx = sx0 + rx, gy = sy0 + ry;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
     if (gx >= 0 && gy >= 0) {
-      if (gx < W - 1 && gy < H) a = ld(vx, P, gx, gy);
-      if (gx < W && gy < H - 1) b = ld(vy, P, gx, gy);
+      if (gx < W - 1 && gy < H) a = *reinterpret_cast<const float4 *>(vx + (size_t)gy * P + gx);
+      if (gx < W && gy < H - 1) b = *reinterpret_cast<const float4 *>(vy + (size_t)gy * P + gx);
+      if (gx + 3 >= W - 1) {
+        if (gx + 1 >= W - 1) a.y = 0.f;
+        if (gx + 2 >= W - 1) a.z = 0.f;
+        a.w = 0.f;
+      }
+      if (gx + 3 >= W) {
+        if (gx + 1 >= W) b.y = 0.f;
+        if (gx + 2 >= W) b.z = 0.f;
+        b.w = 0.f;
+      }
     }
-    sxv[i] = a;
-    syv[i] = b;
+    *reinterpret_cast<float4 *>(sxv + ry * AD_SW + rx) = a;
+    *reinterpret_cast<float4 *>(syv + ry * AD_SW + rx) = b;
   }
-  for (int i = tid; i < AD_TX * AD_TY; i += 256) {
-    int ty = i / AD_TX, tx = i - ty * AD_TX;
-    int x = X0 + tx, y = Y0 + ty;
-    uint8_t a = 0, b = 0;
+  for (int i = tid; i < AD_TY * (AD_TX / 4); i += 256) {
+    const int ty = i / (AD_TX / 4), tx = 4 * (i - ty * (AD_TX / 4));
+    const int x = X0 + tx, y = Y0 + ty;
+    unsigned a = 0u, b = 0u;
     if (x < W && y < H) {
-      a = __ldg(v.cx + (size_t)y * P + x);
-      b = __ldg(v.cy + (size_t)y * P + x);
+      a = __ldg(reinterpret_cast<const unsigned *>(v.cx + (size_t)y * P + x));
+      b = __ldg(reinterpret_cast<const unsigned *>(v.cy + (size_t)y * P + x));
     }
-    scx[i] = a;
-    scy[i] = b;
+    *reinterpret_cast<unsigned *>(scx + ty * AD_TX + tx) = a;
+    *reinterpret_cast<unsigned *>(scy + ty * AD_TX + tx) = b;
   }
   __syncthreads();
   const Win wx{sxv, sx0, sy0}, wy{syv, sx0, sy0};
