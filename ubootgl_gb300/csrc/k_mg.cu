@@ -980,7 +980,7 @@ __device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
             int i = y * w + x;
             unsigned ci = c[i];
             T pw = e[i - 1], pe = e[i + 1], ps = e[i - w], pn = e[i + w], fi = f[i];
-            if (__all_sync(__activemask(), ci == (C_CENTER | C_W | C_E | C_S | C_N)))
+            if (ci == (C_CENTER | C_W | C_E | C_S | C_N))
               e[i] = ((((pw + pe) + ps) + pn) + fi * hh * hh) * T(0.25);
             else
               e[i] = rb_update1<T>(ci, pw, pe, ps, pn, fi, hh);
