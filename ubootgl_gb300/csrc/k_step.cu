@@ -259,9 +259,11 @@ __device__ __forceinline__ void k_diffuse_body(VelBufs v, int srcx, int srcy,
   const int x = 4 * (bx * VX + threadIdx.x), y = by * VY + threadIdx.y;
   const int W = v.W, H = v.H, P = v.pitch;
   const float a = sc->a, den = sc->den, rden = sc->rden;
-  if (bz == 0) {
+  // both components per thread (independent arrays; twice the loads in
+  // flight per thread)
+  (void)bz;
+  if ((comps & 1) && y >= 1 && y < H - 1 && x <= W - 3 && x + 3 >= 1) {
     // vx: interior faces x in [1, W-3], y in [1, H-2]
-    if (!(comps & 1) || y < 1 || y >= H - 1 || x > W - 3 || x + 3 < 1) return;
     const float *s = pick(v.vx, srcx);
     float4 C = ld4(s, P, x, y), N = ld4(s, P, x, y + 1), S = ld4(s, P, x, y - 1);
     uchar4 K = __ldg(reinterpret_cast<const uchar4 *>(v.cx + (size_t)y * P + x));
@@ -281,9 +283,9 @@ __device__ __forceinline__ void k_diffuse_body(VelBufs v, int srcx, int srcy,
       o[j] = (k & FC_M) ? div_rn(c + a * val, den, rden) : 0.0f;
     }
     st4_masked(pick(v.vx, 1 - srcx) + (size_t)y * P, x, 1, W - 3, o);
-  } else {
+  }
+  if ((comps & 2) && y >= 1 && y < H - 2 && x <= W - 2 && x + 3 >= 1) {
     // vy: interior faces x in [1, W-2], y in [1, H-3]
-    if (!(comps & 2) || y < 1 || y >= H - 2 || x > W - 2 || x + 3 < 1) return;
     const float *s = pick(v.vy, srcy);
     float4 C = ld4(s, P, x, y), N = ld4(s, P, x, y + 1), S = ld4(s, P, x, y - 1);
     uchar4 K = __ldg(reinterpret_cast<const uchar4 *>(v.cy + (size_t)y * P + x));
@@ -818,7 +820,7 @@ void launch_accum(const VelBufs &v, int fx, int fy, float *ax, float *ay, cudaSt
 void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, int comps,
                           cudaStream_t st) {
   ProfScope ps_(KC_DIFFUSE, st);
-  launch_pdl(k_diffuse, grid_vec(v.W, v.H, 2), dim3(VX, VY), 0, st, v, srcx, srcy, sc, comps);
+  launch_pdl(k_diffuse, grid_vec(v.W, v.H), dim3(VX, VY), 0, st, v, srcx, srcy, sc, comps);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
@@ -909,7 +911,7 @@ int multi_blocks_vbc(const VbcM &a) {
   return (n + 255) / 256;
 }
 int multi_blocks_diffuse(DiffuseM &a) {
-  dim3 g = grid_vec(a.v.W, a.v.H, 2);
+  dim3 g = grid_vec(a.v.W, a.v.H);
   a.gx = (int)g.x;
   a.gy = (int)g.y;
   return (int)(g.x * g.y * g.z);
