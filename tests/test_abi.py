@@ -37,3 +37,23 @@ def test_no_cpu_fallback_without_gpu(lib):
     flag = np.ones((16, 16), np.float32)
     assert lib.ubg_create(L.fptr(flag), 16, 16, 1.0, 1e-4, C.byref(h)) == -2  # ECUDA
     assert b"no CUDA device" in lib.ubg_last_error()
+
+
+def test_server_arguments_without_gpu(lib):
+    """The step server's host-side checks: bad modes and limits are status
+    codes, and a server with no sessions starts and stops without a GPU."""
+    h = C.c_void_p()
+    assert lib.ubg_server_create(1 << 20, 0, C.byref(h)) == -1  # max_active < 1
+    assert lib.ubg_server_create(1 << 20, 4, C.byref(h)) == 0
+    try:
+        assert lib.ubg_server_set_mode(h, 7) == -1
+        assert lib.ubg_server_set_mode(h, 0) == 0  # UBG_SERVE_STREAMS
+        assert lib.ubg_server_set_mode(h, 1) == 0  # UBG_SERVE_FUSED
+        assert lib.ubg_server_set_fuse_cells(h, -1) == -1
+        assert lib.ubg_server_set_fuse_cells(h, 1 << 16) == 0
+        r = C.c_uint64()
+        assert lib.ubg_server_submit(h, 12345, 1, 0.5, C.byref(r)) == -1  # unknown session
+        assert lib.ubg_server_close(h, 12345) == -1
+        assert lib.ubg_server_drain(h) == 0
+    finally:
+        assert lib.ubg_server_destroy(h) == 0

@@ -91,15 +91,17 @@ def test_mixed_precision_sessions(lib):
     srv.close()
 
 
-def test_fused_many_sessions_match_plain_steps(lib):
+@pytest.mark.parametrize("fuse_cells", [None, 50000])
+def test_fused_many_sessions_match_plain_steps(lib, fuse_cells):
     """24 sessions of uneven sizes, requests of 1..8 steps submitted in a
     burst (requests join and leave the fused step at different step
     boundaries): every session ends bit-identical to a plain simulation
-    stepped the same number of times."""
+    stepped the same number of times.  With a 50000-cell fuse limit the
+    larger sessions run as stream requests beside the fused ones."""
     from ubootgl_gb300.simulation import Server, Simulation
     rng = np.random.default_rng(4)
     sizes = [(int(w), int(w) // 2) for w in rng.choice([96, 128, 192, 256, 320, 512, 768], 24)]
-    srv = Server(16 << 30, max_active=24, mode="fused")
+    srv = Server(16 << 30, max_active=24, mode="fused", fuse_cells=fuse_cells)
     sids, total = [], []
     for i, (W, H) in enumerate(sizes):
         sids.append(srv.open(*session_inputs(W, H, 300 + i, 0.5 + 0.05 * i)))
