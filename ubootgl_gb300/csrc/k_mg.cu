@@ -1710,7 +1710,7 @@ void mg_bind(MgHier &mg, int W, int H, float h0, void *arena, size_t bytes) {
   mg.norm = (double *)p;
   mg.post_norm2 = nullptr;
   mg.tail_top = choose_tail(lv, mg.tail_cells);
-  mg.tail_top_fp64 = choose_tail(lv, 2048, 8);
+  mg.tail_top_fp64 = choose_tail(lv, 128, 8);
   mg.lv = lv;
   mg.levels = (int)lv.size();
   mg.arena = nullptr;  // not owned
