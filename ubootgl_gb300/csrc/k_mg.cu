@@ -1380,29 +1380,76 @@ template <class S>
 __global__ void __launch_bounds__(256) k_dc_resid(DcArgs<S> a) {
   griddep_wait();
   using St = Sto<S>;
-  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-  const int w = a.w, h = a.h;
+  // 4 cells per thread (x4 .. x4 + 3 of row y)
+  const int x4 = (blockIdx.x * 32 + threadIdx.x) * 4, y = blockIdx.y * 8 + threadIdx.y;
+  const int w = a.w, h = a.h, P = a.pitch;
   const float is = a.e ? a.sc_in->inv_s : 0.0f;
   auto PV = [&](int xx, int yy) {
     if (yy >= 1 && yy <= h - 2) xx = xx == 0 ? 1 : (xx == w - 1 ? w - 2 : xx);
     if (xx >= 1 && xx <= w - 2) yy = yy == 0 ? 1 : (yy == h - 1 ? h - 2 : yy);
-    size_t i = (size_t)yy * a.pitch + xx;
+    size_t i = (size_t)yy * P + xx;
     float v = __ldg(a.p + i);
     if (a.e) v = v + St::ldg1(a.e + i) * is;
     return v;
   };
-  float rv = 0.0f;
-  if (x < w && y < h) {
-    size_t i = (size_t)y * a.pitch + x;
-    float pc = PV(x, y);
-    a.pout[i] = pc;
-    if (x >= 1 && x < w - 1 && y >= 1 && y < h - 1)
-      rv = resid1<float>(__ldg(a.code + i), pc, PV(x - 1, y), PV(x + 1, y), PV(x, y - 1),
-                         PV(x, y + 1), __ldg(a.f + i), a.ihsq);
-    a.r[i] = rv;
+  float sq = 0.0f;
+  unsigned mb = 0u;
+  if (x4 < w && y < h) {
+    float pc[4], rv[4] = {0.f, 0.f, 0.f, 0.f};
+    const size_t i0 = (size_t)y * P + x4;
+    if (x4 >= 4 && x4 + 4 <= w - 2 && y >= 2 && y <= h - 3) {
+      // interior: no edge mapping; rows y-1, y, y+1 as float4 plus the
+      // west / east neighbours
+      auto row4 = [&](int yy, float *o) {
+        const size_t i = (size_t)yy * P + x4;
+        float4 v = __ldg(reinterpret_cast<const float4 *>(a.p + i));
+        o[0] = v.x;
+        o[1] = v.y;
+        o[2] = v.z;
+        o[3] = v.w;
+        if (a.e) {
+          const float4 e = St::ldg4(a.e + i);
+          o[0] = o[0] + e.x * is;
+          o[1] = o[1] + e.y * is;
+          o[2] = o[2] + e.z * is;
+          o[3] = o[3] + e.w * is;
+        }
+      };
+      float s4[4], n4[4];
+      row4(y, pc);
+      row4(y - 1, s4);
+      row4(y + 1, n4);
+      const float pw = PV(x4 - 1, y), pe = PV(x4 + 4, y);
+      const float4 fv = __ldg(reinterpret_cast<const float4 *>(a.f + i0));
+      const uchar4 cv = __ldg(reinterpret_cast<const uchar4 *>(a.code + i0));
+      const float F4[4] = {fv.x, fv.y, fv.z, fv.w};
+      const unsigned C4[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        rv[j] = resid1<float>(C4[j], pc[j], j > 0 ? pc[j - 1] : pw, j < 3 ? pc[j + 1] : pe, s4[j],
+                              n4[j], F4[j], a.ihsq);
+      *reinterpret_cast<float4 *>(a.pout + i0) = make_float4(pc[0], pc[1], pc[2], pc[3]);
+      *reinterpret_cast<float4 *>(a.r + i0) = make_float4(rv[0], rv[1], rv[2], rv[3]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int x = x4 + j;
+        if (x >= w) break;
+        const size_t i = i0 + j;
+        pc[j] = PV(x, y);
+        a.pout[i] = pc[j];
+        if (x >= 1 && x < w - 1 && y >= 1 && y < h - 1)
+          rv[j] = resid1<float>(__ldg(a.code + i), pc[j], PV(x - 1, y), PV(x + 1, y),
+                                PV(x, y - 1), PV(x, y + 1), __ldg(a.f + i), a.ihsq);
+        a.r[i] = rv[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      sq = __fmaf_rn(rv[j], rv[j], sq);
+      mb = max(mb, __float_as_uint(fabsf(rv[j])));
+    }
   }
-  float sq = rv * rv;
-  unsigned mb = __float_as_uint(fabsf(rv));
   for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
   mb = __reduce_max_sync(0xffffffffu, mb);
   __shared__ double red[8];
@@ -1600,7 +1647,7 @@ void dc_resid(MgHier &mg, MgLow &lo, const S *e, cudaStream_t st) {
   a.ihsq = 1.0f / L.hh / L.hh;
   a.r = lo.r32;
   a.sc = lo.dev;
-  dim3 grid((L.w + 31) / 32, (L.h + 7) / 8);
+  dim3 grid((L.w + 127) / 128, (L.h + 7) / 8);
   k_dc_resid<S><<<grid, dim3(32, 8), 0, st>>>(a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
