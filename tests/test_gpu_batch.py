@@ -156,3 +156,25 @@ def test_hybrid_batch_fused_and_branches(lib):
     batch.close()
     for s in alone + members:
         s.close()
+
+
+def test_fused_batch_odd_sizes(lib):
+    """Fused members whose widths leave every remainder modulo 8 and odd
+    heights: bit-identical to stepping alone."""
+    from ubootgl_gb300.simulation import Batch
+    sizes = [(97, 49), (131, 67), (202, 101), (259, 130), (333, 111), (64, 33), (75, 41),
+             (150, 75)]
+    alone = [build(W, H, 500 + i, u_in=0.7 + 0.05 * i) for i, (W, H) in enumerate(sizes)]
+    members = [build(W, H, 500 + i, u_in=0.7 + 0.05 * i) for i, (W, H) in enumerate(sizes)]
+    batch = Batch(members)
+    for _ in range(4):
+        for s in alone:
+            s.step_cfl(0.5)
+        batch.step(cfl=0.5)
+    batch.sync()
+    for a, b in zip(alone, members):
+        for n in ("vx", "vy", "vx_back", "vy_back", "p"):
+            assert np.array_equal(a.get(n), b.get(n)), (a.width, n)
+    batch.close()
+    for s in alone + members:
+        s.close()

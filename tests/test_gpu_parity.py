@@ -77,6 +77,23 @@ def test_steps_bit_exact(lib, W, H):
         assert_same(sim, ref, names=("vx", "vy", "p"), ctx="step %d" % k)
 
 
+# Widths at every remainder modulo 8 (the smoother loads 8-cell groups and
+# the restriction writes 4 coarse cells at a time; advect stages 4-entry
+# vectors), a tall narrow grid and tiny grids near the multigrid's limits.
+EDGE_SIZES = [(131, 67), (134, 70), (135, 35), (45, 200), (12, 10), (9, 9), (36, 18),
+              (1001, 11)]
+
+
+@pytest.mark.parametrize("W,H", EDGE_SIZES)
+def test_steps_bit_exact_edge_sizes(lib, W, H):
+    sim, ref, flag = make_pair(W, H, seed=W + 11, ndisc=3)
+    for k in range(3):
+        dt = WL.cfl_dt(ref.get("vx"), ref.get("vy"), ref.h)
+        sim.step(float(dt))
+        ref.step(dt)
+        assert_same(sim, ref, names=("vx", "vy", "p"), ctx="%dx%d step %d" % (W, H, k))
+
+
 def test_graph_matches_direct(lib):
     W, H = 130, 66
     a, ref, flag = make_pair(W, H, seed=3)
