@@ -1660,6 +1660,9 @@ void FusedStepper::join(ubg_sim *s) {
   s->io_consume();
   bool accum = s->accum_dirty;
   if (accum) s->apply_accum();
+  // max|u| of the current fields for the first fused step's dt (the
+  // scalars this also writes are recomputed by that step's own CFL launch
+  // with the request's factor)
   if (!s->umax_ready || accum)
     launch_cfl(s->v, s->fx, s->fy, 0.5f, s->h, s->mu, s->pwidth, s->d_umax, s->d_sc, s->st, false);
   s->umax_ready = true;
