@@ -248,11 +248,20 @@ def run_ours(args):
     if rank != 0:
         return
 
-    # ---- the mixed-precision solver on the same workload (extension)
+    # ---- the solver modes on the same workload (extensions): the tolerance
+    # solver in FP32 / FP16 / BF16 to the same relative residual, and the
+    # fixed two-cycle mixed solvers
     modes = {}
+    if args.tol_steps > 0:
+        for prec in ("fp32", "fp16", "bf16"):
+            modes["tol_" + prec] = time_tolerance(L, lib, flag, vx, vy, prec, args.tol_steps,
+                                                  args.warmup, dev, args.tol)
+        base = modes["tol_fp32"]["value"]
+        for prec in ("fp16", "bf16"):
+            modes["tol_" + prec]["vs_fp32_at_equal_tol"] = round(modes["tol_" + prec]["value"] / base, 3)
     if args.mode_steps > 0:
         for prec in ("fp16", "bf16"):
-            modes["mixed_" + prec] = time_mode(L, lib, flag, vx, vy, prec, args.mode_steps,
+            modes["fixed_" + prec] = time_mode(L, lib, flag, vx, vy, prec, args.mode_steps,
                                                args.warmup, dev)
 
     # ---- batched uneven instances and the served stream (extensions)
@@ -280,7 +289,8 @@ def run_ours(args):
         "config": {"workload": "fluid step %dx%d, 12 discs, FP32, 2 V-cycles, dt=0.5h/max|u| on device"
                                % (W, H),
                    "solver": "FP32 drop-in: the reference's step with its 2 V-cycles (value); "
-                             "mixed FP16/BF16 solvers in modes; served stream in served",
+                             "tolerance solver (FP32 / FP16 / BF16 coarse levels, residual "
+                             "<= tol) and fixed mixed solvers in modes; served stream in served",
                    "grid": [W, H], "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2: step working set %.0f MB > 129 MB"
                          % (working_set_bytes(W, H) / 1e6)},
@@ -303,6 +313,49 @@ def run_ours(args):
                                 "cores": info["cores"], "kind": info["kind"],
                                 "sample": info["sample"]}
     print(json.dumps(line), flush=True)
+
+
+def time_tolerance(L, lib, flag, vx, vy, precision, steps, warmup, dev, tol):
+    """Whole steps with the tolerance solver (flexible CG preconditioned by
+    the tolerance hierarchy's V-cycle, coarse levels in `precision`) until
+    ||r|| <= tol ||f_c|| every projection; CUDA events on the simulation's
+    stream around `steps` steps (the solver synchronises once per V-cycle to
+    test the residual, inside the timed region)."""
+    import ctypes as C
+    import torch
+    from ubootgl_gb300.simulation import Simulation
+    H, W = flag.shape
+    sim = Simulation(flag, 1.0, 1e-4)
+    sim.set_options(solver_mode=L.SOLVE_TOLERANCE, tol=tol, max_vcycles=200, precision=precision)
+    for n, a in (("vx", vx), ("vy", vy), ("vx_back", vx), ("vy_back", vy)):
+        sim.set(n, a)
+    stream = C.c_void_p()
+    L.check(lib.ubg_stream(sim._h, C.byref(stream)))
+    ext = torch.cuda.ExternalStream(stream.value, device=dev)
+    for _ in range(max(3, warmup)):
+        sim.step_cfl(0.5)
+    sim.sync()
+    cycles, rels = [], []
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(steps):
+        sim.step_cfl(0.5)
+        c, r = sim.solver_stats()
+        cycles.append(c)
+        rels.append(r)
+    e1.record(ext)
+    sim.sync()
+    ms = e0.elapsed_time(e1)
+    finite = bool(np.isfinite(sim.get("p")).all())
+    sim.close()
+    return {"value": round(W * H * steps / (ms / 1e3) / 1e6, 2), "unit": "Mcell-steps/s",
+            "ms_per_step": round(ms / steps, 4), "steps": steps, "tol": tol,
+            "vcycles_per_projection": round(float(np.mean(cycles)), 2),
+            "vcycles_max": int(max(cycles)), "residual_max": float("%.3e" % max(rels)),
+            "solver": "flexible CG (FP64 pressure, FP32 vectors, FP64 norms) preconditioned by "
+                      "one V-cycle: level 0 FP32, coarse levels %s" % precision,
+            "fields_finite": finite}
 
 
 def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev):
@@ -645,7 +698,11 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=30)
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--mode-steps", type=int, default=500,
-                    help="timed steps per mixed-precision mode (0: skip)")
+                    help="timed steps per fixed-mode mixed-precision solver (0: skip)")
+    ap.add_argument("--tol-steps", type=int, default=10,
+                    help="timed steps per tolerance-mode precision (0: skip)")
+    ap.add_argument("--tol", type=float, default=1e-6,
+                    help="relative residual of the tolerance modes")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batch", type=int, default=64, help="batched instances (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=50)

@@ -98,7 +98,8 @@ struct ubg_sim {
   float *ax = nullptr, *ay = nullptr;
   uint8_t *codes_x = nullptr, *codes_y = nullptr;
   MgHier mg;
-  MgLow lo;  // 16-bit correction hierarchy of the mixed-precision modes
+  MgLow lo;       // 16-bit correction hierarchy of the fixed-mode mixed solver
+  FcgSolver fcg;  // tolerance-mode solver (allocated when that mode is set)
   StepScalars *d_sc = nullptr;
   unsigned int *d_umax = nullptr;
   SinkCell *d_sinks = nullptr;
@@ -195,6 +196,7 @@ struct ubg_sim {
   // The flag changed on the device: coarse flags and every stencil code
   // (MG::updateFields on the device flag, plus the face codes).
   void flag_changed() {
+    fcg.dirty = true;
     mg_update_fields(mg, st);
     launch_face_codes(v, flag(), codes_x, codes_y, st);
     umax_ready = false;
@@ -212,6 +214,7 @@ struct ubg_sim {
     if (h_sinks) cudaFreeHost(h_sinks);
     if (h_norm) cudaFreeHost(h_norm);
     mg_low_free(lo);
+    fcg_free(fcg);
     if (scratch) cudaFree(scratch);
     if (io_st) cudaStreamSynchronize(io_st);
     if (io_out_st) cudaStreamSynchronize(io_out_st);
@@ -295,62 +298,39 @@ struct ubg_sim {
       solve_mixed();
       return;
     }
-    if (opt.solver_mode == UBG_SOLVE_TOLERANCE) {
-      solve_tolerance();
-      return;
-    }
     for (int c = 0; c < opt.vcycles; c++) mg_solve(mg, true, st);
     last_vcycles = opt.vcycles;
     last_rel = -1.0;
   }
 
-  // Extension: FP32 defect correction around a 16-bit V-cycle.  Fixed mode:
+  // Extension, fixed mode: FP32 defect correction around a 16-bit V-cycle,
   // `vcycles` corrections (no host synchronisation, capturable), equal in
-  // exact arithmetic to `vcycles` V-cycles started from p with zero-gradient
-  // edges.  Tolerance mode: on the compatible system (mean-free f).
+  // exact arithmetic to `vcycles` V-cycles started from p with
+  // zero-gradient edges.
   void solve_mixed() {
     if (lo.levels != mg.levels || lo.prec != opt.precision)
       throw std::runtime_error("mixed-precision hierarchy not allocated (ubg_set_options)");
-    if (opt.solver_mode == UBG_SOLVE_TOLERANCE) {
-      double fnorm2 = mg_meanfree_rhs(mg, st, true);
-      last_vcycles = mg_solve_mixed(mg, lo, opt.tol, opt.max_vcycles, fnorm2, &last_rel, st);
-    } else {
-      last_vcycles = mg_solve_mixed(mg, lo, 0.0, opt.vcycles, 0.0, nullptr, st);
-      last_rel = -1.0;
-    }
-  }
-
-  // Extension: V-cycles until ||r|| <= tol * ||f|| (FP64 norms) on the
-  // compatible part of the system (f minus its mean over the interior fluid
-  // cells; the zero-gradient system is singular).
-  void solve_tolerance() {
-    MgLevel &L0 = mg.lv[0];
-    int c = 0;
-    double fnorm2 = mg_meanfree_rhs(mg, st, true);
-    double target2 = (double)opt.tol * (double)opt.tol * fnorm2;
-    for (c = 0; c < opt.max_vcycles; c++) {
-      // the level-0 post-smoothing launch returns ||r||^2 of its result
-      UBG_CUDA(cudaMemsetAsync(mg.norm, 0, sizeof(double), st));
-      mg.post_norm2 = mg.levels > 2 ? mg.norm : nullptr;
-      mg_solve(mg, true, st);
-      mg.post_norm2 = nullptr;
-      if (mg.levels <= 2) level_residual(L0, mg.cur0, nullptr, mg.norm, st);
-      UBG_CUDA(cudaMemcpyAsync(h_norm, mg.norm, sizeof(double), cudaMemcpyDeviceToHost, st));
-      UBG_CUDA(cudaStreamSynchronize(st));
-      if (*h_norm <= target2) {
-        c++;
-        break;
-      }
-    }
-    last_vcycles = c;
-    last_rel = std::sqrt(*h_norm / (fnorm2 > 0.0 ? fnorm2 : 1.0));
+    last_vcycles = mg_solve_mixed(mg, lo, 0.0, opt.vcycles, 0.0, nullptr, st);
+    last_rel = -1.0;
   }
 
   // project(), simulation.cpp:164-208 (without the trailing setVBCs of step).
   // The gradient kernel also starts the max|u| reduction for the next CFL dt.
+  // Tolerance mode (extension): flexible CG preconditioned by the tolerance
+  // hierarchy's V-cycle (k_krylov.cu) until ||r|| <= tol ||f_c||; the
+  // gradient update reads its FP64 pressure.
   void project(int nsink_cells) {
     launch_divergence(v, fx, fy, f(), d_sc, st);
     launch_sinks(f(), P, d_sinks, nsink_cells, st);
+    if (opt.solver_mode == UBG_SOLVE_TOLERANCE) {
+      if (!fcg.arena) throw std::runtime_error("tolerance solver not allocated (ubg_set_options)");
+      fcg_set_precision(fcg, opt.precision);
+      last_vcycles = fcg_solve(fcg, flag(), f(), p(), (double)opt.tol, opt.max_vcycles, &last_rel, st);
+      launch_pbc(p(), P, W, H, bc, st);
+      UBG_CUDA(cudaMemsetAsync(d_umax, 0, sizeof(unsigned int), st));
+      launch_gradient64(v, fx, fy, fcg.x, d_sc, d_umax, st);
+      return;
+    }
     solve_pressure();
     launch_pbc(p(), P, W, H, bc, st);
     UBG_CUDA(cudaMemsetAsync(d_umax, 0, sizeof(unsigned int), st));
@@ -640,10 +620,19 @@ int ubg_set_options(ubg_sim *s, const ubg_options *o) {
       throw ArgError("precision");
     if (o->solver_mode == UBG_SOLVE_TOLERANCE && !(o->tol > 0.0f)) throw ArgError("tol must be > 0");
     UBG_CUDA(cudaStreamSynchronize(s->st));
-    if (o->precision == UBG_FP32)
+    if (o->solver_mode == UBG_SOLVE_TOLERANCE) {
+      // flexible CG over the tolerance hierarchy; the fixed-mode 16-bit
+      // hierarchy is not needed
       mg_low_free(s->lo);
-    else if (s->lo.prec != o->precision || s->lo.levels != s->mg.levels)
-      mg_low_alloc(s->lo, s->mg, o->precision);
+      if (!s->fcg.arena) fcg_alloc(s->fcg, s->W, s->H, s->P, s->h);
+      fcg_set_precision(s->fcg, o->precision);
+    } else {
+      fcg_free(s->fcg);
+      if (o->precision == UBG_FP32)
+        mg_low_free(s->lo);
+      else if (s->lo.prec != o->precision || s->lo.levels != s->mg.levels)
+        mg_low_alloc(s->lo, s->mg, o->precision);
+    }
     s->opt = *o;
     s->gen++;
     return UBG_OK;
@@ -771,8 +760,7 @@ int ubg_upload(ubg_sim *s, int field, const float *src) {
     if (field == UBG_FLAG) {
       upload_flag_u8(s->mg.lv[0], src, s->W, s->H, s->st);
       s->flag_host.assign(src, src + (size_t)s->W * s->H);
-      mg_update_fields(s->mg, s->st);
-      launch_face_codes(s->v, s->flag(), s->codes_x, s->codes_y, s->st);
+      s->flag_changed();
       s->sync();
       return UBG_OK;
     }
@@ -2097,7 +2085,9 @@ int ubg_sim_device_bytes(ubg_sim *s, size_t *bytes) {
       for (auto &L : s->mg.lv) lo += 3 * (((size_t)L.pitch * L.h * 2 + 255) / 256 * 256);
       lo += ((size_t)s->P * s->H * 4 + 255) / 256 * 256 + 256;
     }
-    *bytes = s->arena_bytes + s->mg.arena_bytes + lo + s->scratch_bytes;
+    size_t fb = 0;
+    if (s->fcg.arena) fb = fcg_bytes(s->W, s->H, s->P, s->fcg.prec);
+    *bytes = s->arena_bytes + s->mg.arena_bytes + lo + fb + s->scratch_bytes;
     return UBG_OK;
   });
 }

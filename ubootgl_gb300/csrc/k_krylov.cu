@@ -1,0 +1,543 @@
+// Tolerance-mode pressure solver: flexible conjugate gradients (FCG(1),
+// Y. Notay, "Flexible conjugate gradients", SIAM J. Sci. Comput. 22(4),
+// 2000) on the zero-gradient pressure system of MG::solve
+// (pressure_solver.cpp:91-116: r = f + (1/h^2) sum_n flag_n (p_n - p) on
+// the interior fluid cells), preconditioned by one V-cycle of the
+// tolerance hierarchy (ext_vcycle, k_mg.cu), run until
+// ||r|| <= tol ||f_c|| in FP64 norms.
+//
+// The reference always runs two V-cycles and never reaches a tolerance
+// (simulation.cpp:189-190); this solver is the extension that does.
+//
+// Precision: the pressure iterate x is FP64.  Rounding p to FP32 alone
+// leaves a relative residual of 2e-4 at 512x256 and 6e-4 at 1024x512 for a
+// flow state's pressure (its smooth part is large against the neighbour
+// differences the residual is made of), so no FP32 p reaches 1e-6.  The
+// Krylov vectors r, d, q and the preconditioner output z are FP32; the
+// neighbour differences of x are taken in FP64 and rounded once; dot
+// products and norms are FP64 across warps.  The V-cycle runs its level 0
+// in FP32 and its coarse levels in FP32, FP16 or BF16 (ubg_options
+// precision).
+//
+// Compatibility: the system is singular (constants on each connected fluid
+// region), and f sums to the net flux through the domain edges, which is
+// not zero when inflow and outflow differ.  The solver moves that sum to
+// the outflow column x = W-2 (f_c = f - sum(f) / n on its n fluid cells;
+// all fluid cells when that column has none), where the reference's
+// outflow boundary (setVBCs, simulation.cpp:80-102) takes up the
+// imbalance.  Enclosed pockets have zero net flux and keep their f.
+#include "ubg_internal.cuh"
+
+#include <cmath>
+#include <cstring>
+
+namespace ubg {
+namespace {
+
+constexpr int BX = 32, BY = 8;  // 32 x 8 threads, 4 cells of a row per thread
+
+__device__ __forceinline__ bool interior(int x, int y, int W, int H) {
+  return x >= 1 && x < W - 1 && y >= 1 && y < H - 1;
+}
+
+// a + b = s + e exactly (Knuth's TwoSum; the library is built without FMA
+// contraction, so every operation rounds as written).
+__device__ __forceinline__ float two_sum(float a, float b, float *e) {
+  const float s = a + b, bb = s - a;
+  *e = (a - (s - bb)) + (b - bb);
+  return s;
+}
+// a + b + c + d with the rounding errors of the three additions added back:
+// the stencil's neighbour differences are exact in FP32 but cancel in the
+// sum by orders of magnitude for a smooth field, so a plain FP32 sum loses
+// the digits the residual is made of.
+__device__ __forceinline__ float sum4(float a, float b, float c, float d) {
+  float e1, e2, e3;
+  const float s1 = two_sum(a, b, &e1), s2 = two_sum(c, d, &e2);
+  const float s = two_sum(s1, s2, &e3);
+  return s + ((e1 + e2) + e3);
+}
+
+// Block sums of up to three doubles and a max, then one atomic each.
+template <int N>
+__device__ __forceinline__ void block_reduce(double (&v)[N], unsigned mx, double *const (&dst)[N],
+                                             unsigned *mdst) {
+  const int tid = threadIdx.y * BX + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < N; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  __shared__ double red[N][BY];
+  __shared__ unsigned redm[BY];
+  if ((tid & 31) == 0) {
+#pragma unroll
+    for (int k = 0; k < N; k++) red[k][tid >> 5] = v[k];
+    redm[tid >> 5] = mx;
+  }
+  __syncthreads();
+  if (tid == 0) {
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      double t = 0.0;
+      for (int i = 0; i < BY; i++) t += red[k][i];
+      if (dst[k]) atomicAdd(dst[k], t);
+    }
+    if (mdst) {
+      unsigned m = 0;
+      for (int i = 0; i < BY; i++) m = max(m, redm[i]);
+      atomicMax(mdst, m);
+    }
+  }
+}
+
+// Sum of f over the interior fluid cells, the fluid cells of the outflow
+// column x = W-2 and all interior fluid cells (counts).
+__global__ void __launch_bounds__(BX *BY) k_fcg_fsum(const float *__restrict__ f,
+                                                     const uint8_t *__restrict__ code, int W,
+                                                     int H, int P, FcgScalars *sc) {
+  griddep_wait();
+  const int x4 = (blockIdx.x * BX + threadIdx.x) * 4, y = blockIdx.y * BY + threadIdx.y;
+  float s = 0.0f;
+  int ne = 0, nf = 0;
+  if (y >= 1 && y < H - 1) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int x = x4 + j;
+      if (x >= 1 && x < W - 1) {
+        const size_t i = (size_t)y * P + x;
+        if (__ldg(code + i) & 1u) {
+          s += __ldg(f + i);
+          nf++;
+          if (x == W - 2) ne++;
+        }
+      }
+    }
+  }
+  double v[3] = {(double)s, (double)ne, (double)nf};
+  double *const dst[3] = {&sc->fsum, &sc->neast, &sc->nfluid};
+  block_reduce<3>(v, 0u, dst, nullptr);
+}
+
+__device__ __forceinline__ double compat_corr(const FcgScalars *sc, int x, int W) {
+  const double ne = sc->neast, nf = sc->nfluid;
+  if (ne > 0.0) return x == W - 2 ? sc->fsum / ne : 0.0;
+  return nf > 0.0 ? sc->fsum / nf : 0.0;
+}
+
+// r = f_c + ihsq * (float)(sum_n flag_n (x_n - x)) on the interior fluid
+// cells (0 elsewhere), the neighbour sum in FP64; neighbours on the domain
+// edge are zero-gradient copies (difference 0).  Writes r and accumulates ||r||^2 and max|r|, and
+// with want_ff also ||f_c||^2.
+__global__ void __launch_bounds__(BX *BY) k_fcg_resid(const double *__restrict__ xv,
+                                                      const float *__restrict__ f,
+                                                      const uint8_t *__restrict__ code, int W,
+                                                      int H, int P, float ihsq, float *r,
+                                                      FcgScalars *sc, int want_ff) {
+  griddep_wait();
+  const int x4 = (blockIdx.x * BX + threadIdx.x) * 4, y = blockIdx.y * BY + threadIdx.y;
+  float ff = 0.0f, rr = 0.0f;
+  unsigned mx = 0;
+  if (x4 < W && y < H) {
+    float rv[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int x = x4 + j;
+      if (x >= W || !interior(x, y, W, H)) continue;
+      const size_t i = (size_t)y * P + x;
+      const unsigned c = __ldg(code + i);
+      if (!(c & 1u)) continue;
+      const double xc = __ldg(xv + i);
+      double sum = 0.0;
+      if ((c & 2u) && x - 1 >= 1) sum += __ldg(xv + i - 1) - xc;
+      if ((c & 4u) && x + 1 < W - 1) sum += __ldg(xv + i + 1) - xc;
+      if ((c & 8u) && y - 1 >= 1) sum += __ldg(xv + i - P) - xc;
+      if ((c & 16u) && y + 1 < H - 1) sum += __ldg(xv + i + P) - xc;
+      const float fc = (float)((double)__ldg(f + i) - compat_corr(sc, x, W));
+      rv[j] = fc + ihsq * (float)sum;
+      ff = __fmaf_rn(fc, fc, ff);
+      rr = __fmaf_rn(rv[j], rv[j], rr);
+      mx = max(mx, __float_as_uint(fabsf(rv[j])));
+    }
+    float *o = r + (size_t)y * P + x4;
+    if (x4 + 3 < W) {
+      *reinterpret_cast<float4 *>(o) = make_float4(rv[0], rv[1], rv[2], rv[3]);
+    } else {
+      for (int j = 0; j < 4 && x4 + j < W; j++) o[j] = rv[j];
+    }
+  }
+  double v[2] = {(double)ff, (double)rr};
+  double *const dst[2] = {want_ff ? &sc->ff : nullptr, &sc->rr};
+  block_reduce<2>(v, mx, dst, &sc->maxbits);
+}
+
+// zq = (z, q_prev); zeroes the accumulators of k_fcg_dir.
+__global__ void __launch_bounds__(BX *BY) k_fcg_zq(const float *__restrict__ z,
+                                                   const float *__restrict__ q, int W, int H,
+                                                   int P, FcgScalars *sc, int slot) {
+  griddep_wait();
+  const int x4 = (blockIdx.x * BX + threadIdx.x) * 4, y = blockIdx.y * BY + threadIdx.y;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    sc->dq[slot] = 0.0;
+    sc->dr = 0.0;
+  }
+  float s = 0.0f;
+  if (x4 < W && y < H) {
+    const size_t i = (size_t)y * P + x4;
+    const float4 a = *reinterpret_cast<const float4 *>(z + i);
+    const float4 b = *reinterpret_cast<const float4 *>(q + i);
+    // q is 0 outside the interior fluid cells and beyond the width
+    s = a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+  }
+  double v[1] = {(double)s};
+  double *const dst[1] = {&sc->zq};
+  block_reduce<1>(v, 0u, dst, nullptr);
+}
+
+// d = z + beta d_old (beta = -zq / dq_prev; 0 on the first iteration) on
+// every cell, q = A d = -ihsq * sum_n flag_n (d_n - d) on the interior
+// fluid cells (0 elsewhere), (d, q) and (d, r); zeroes the accumulators of
+// k_fcg_update.
+__global__ void __launch_bounds__(BX *BY) k_fcg_dir(const float *__restrict__ z,
+                                                    const float *__restrict__ dold, float *dnew,
+                                                    float *q, const float *__restrict__ r,
+                                                    const uint8_t *__restrict__ code, int W,
+                                                    int H, int P, float ihsq, FcgScalars *sc,
+                                                    int first, int slot) {
+  griddep_wait();
+  const int x4 = (blockIdx.x * BX + threadIdx.x) * 4, y = blockIdx.y * BY + threadIdx.y;
+  const float beta = first ? 0.0f : (float)(-sc->zq / sc->dq[slot ^ 1]);
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    sc->rr = 0.0;
+    sc->maxbits = 0u;
+  }
+  float dq = 0.0f, dr = 0.0f;
+  if (x4 < W && y < H) {
+    auto D = [&](size_t i) { return first ? __ldg(z + i) : __ldg(z + i) + beta * __ldg(dold + i); };
+    const size_t i0 = (size_t)y * P + x4;
+    float dc[4], qv[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < 4; j++) dc[j] = (x4 + j < W) ? D(i0 + j) : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int x = x4 + j;
+      if (x >= W || !interior(x, y, W, H)) continue;
+      const size_t i = i0 + j;
+      const unsigned c = __ldg(code + i);
+      if (!(c & 1u)) continue;
+      const float a0 = ((c & 2u) && x - 1 >= 1) ? (j > 0 ? dc[j - 1] : D(i - 1)) - dc[j] : 0.0f;
+      const float a1 = ((c & 4u) && x + 1 < W - 1) ? (j < 3 ? dc[j + 1] : D(i + 1)) - dc[j] : 0.0f;
+      const float a2 = ((c & 8u) && y - 1 >= 1) ? D(i - P) - dc[j] : 0.0f;
+      const float a3 = ((c & 16u) && y + 1 < H - 1) ? D(i + P) - dc[j] : 0.0f;
+      qv[j] = -ihsq * sum4(a0, a1, a2, a3);
+      dq = __fmaf_rn(dc[j], qv[j], dq);
+      dr = __fmaf_rn(dc[j], __ldg(r + i), dr);
+    }
+    if (x4 + 3 < W) {
+      *reinterpret_cast<float4 *>(dnew + i0) = make_float4(dc[0], dc[1], dc[2], dc[3]);
+      *reinterpret_cast<float4 *>(q + i0) = make_float4(qv[0], qv[1], qv[2], qv[3]);
+    } else {
+      for (int j = 0; j < 4 && x4 + j < W; j++) {
+        dnew[i0 + j] = dc[j];
+        q[i0 + j] = qv[j];
+      }
+    }
+  }
+  double v[2] = {(double)dq, (double)dr};
+  double *const dst[2] = {&sc->dq[slot], &sc->dr};
+  block_reduce<2>(v, 0u, dst, nullptr);
+}
+
+// alpha = dr / dq; x += alpha d; r -= alpha q; ||r||^2 and max|r|; zeroes
+// the accumulator of the next k_fcg_zq.
+__global__ void __launch_bounds__(BX *BY) k_fcg_update(double *xv, const float *__restrict__ d,
+                                                       float *r, const float *__restrict__ q,
+                                                       int W, int H, int P, FcgScalars *sc,
+                                                       int slot) {
+  griddep_wait();
+  const int x4 = (blockIdx.x * BX + threadIdx.x) * 4, y = blockIdx.y * BY + threadIdx.y;
+  const double dqv = sc->dq[slot];
+  const double alpha = dqv != 0.0 ? sc->dr / dqv : 0.0;
+  const float af = (float)alpha;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) sc->zq = 0.0;
+  float rr = 0.0f;
+  unsigned mx = 0;
+  if (x4 < W && y < H) {
+    const size_t i0 = (size_t)y * P + x4;
+    if (x4 + 3 < W) {
+      const float4 dv = *reinterpret_cast<const float4 *>(d + i0);
+      const float4 qv = *reinterpret_cast<const float4 *>(q + i0);
+      float4 rv = *reinterpret_cast<const float4 *>(r + i0);
+      double2 xa = *reinterpret_cast<const double2 *>(xv + i0);
+      double2 xb = *reinterpret_cast<const double2 *>(xv + i0 + 2);
+      xa.x += alpha * (double)dv.x;
+      xa.y += alpha * (double)dv.y;
+      xb.x += alpha * (double)dv.z;
+      xb.y += alpha * (double)dv.w;
+      *reinterpret_cast<double2 *>(xv + i0) = xa;
+      *reinterpret_cast<double2 *>(xv + i0 + 2) = xb;
+      rv.x -= af * qv.x;
+      rv.y -= af * qv.y;
+      rv.z -= af * qv.z;
+      rv.w -= af * qv.w;
+      *reinterpret_cast<float4 *>(r + i0) = rv;
+      const float R[4] = {rv.x, rv.y, rv.z, rv.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        rr = __fmaf_rn(R[j], R[j], rr);
+        mx = max(mx, __float_as_uint(fabsf(R[j])));
+      }
+    } else {
+      for (int j = 0; j < 4 && x4 + j < W; j++) {
+        const size_t i = i0 + j;
+        xv[i] += alpha * (double)d[i];
+        const float rj = r[i] - af * q[i];
+        r[i] = rj;
+        rr = __fmaf_rn(rj, rj, rr);
+        mx = max(mx, __float_as_uint(fabsf(rj)));
+      }
+    }
+  }
+  double v[1] = {(double)rr};
+  double *const dst[1] = {&sc->rr};
+  block_reduce<1>(v, mx, dst, &sc->maxbits);
+}
+
+// x = (double)p on every cell (warm start from the current pressure).
+__global__ void __launch_bounds__(BX *BY) k_fcg_load(const float *__restrict__ p, double *xv, int W,
+                                                     int H, int P) {
+  griddep_wait();
+  const int x4 = (blockIdx.x * BX + threadIdx.x) * 4, y = blockIdx.y * BY + threadIdx.y;
+  if (x4 >= W || y >= H) return;
+  const size_t i = (size_t)y * P + x4;
+  for (int j = 0; j < 4 && x4 + j < W; j++) xv[i + j] = (double)p[i + j];
+}
+
+// p = (float)x on the interior cells (the edges are set by setPBC next).
+__global__ void __launch_bounds__(BX *BY) k_fcg_store(const double *__restrict__ xv, float *p,
+                                                      int W, int H, int P) {
+  griddep_wait();
+  const int x4 = (blockIdx.x * BX + threadIdx.x) * 4, y = blockIdx.y * BY + threadIdx.y;
+  if (y < 1 || y >= H - 1) return;
+  const size_t i = (size_t)y * P + x4;
+  for (int j = 0; j < 4; j++) {
+    const int x = x4 + j;
+    if (x >= 1 && x < W - 1) p[i + j] = (float)xv[i + j];
+  }
+}
+
+// The pressure-gradient update (simulation.cpp:196-207) from the FP64
+// pressure: vx -= ih * (float)(x(x+1) - x(x)) on the faces whose two cells
+// are fluid, x in [1, W-3]; vy likewise, y in [1, H-3].  max|u| of the
+// interior faces in range is folded into *umax_bits.
+__global__ void __launch_bounds__(BX *BY) k_gradient64(float *vx, float *vy,
+                                                       const uint8_t *__restrict__ cx,
+                                                       const uint8_t *__restrict__ cy,
+                                                       const double *__restrict__ xv, int W, int H,
+                                                       int P, const StepScalars *__restrict__ sc,
+                                                       unsigned *umax_bits) {
+  griddep_wait();
+  const int x4 = (blockIdx.x * BX + threadIdx.x) * 4, y = blockIdx.y * BY + threadIdx.y;
+  float m = 0.0f;
+  if (y >= 1 && y < H - 1) {
+    const float ih = sc->ih;
+    for (int j = 0; j < 4; j++) {
+      const int x = x4 + j;
+      const size_t i = (size_t)y * P + x;
+      if (x >= 1 && x <= W - 3) {
+        float u = vx[i];
+        if (__ldg(cx + i) & FC_M) u = u - ih * (float)(__ldg(xv + i + 1) - __ldg(xv + i));
+        vx[i] = u;
+        m = fmaxf(m, fabsf(u));
+      }
+      if (x >= 1 && x <= W - 2 && y <= H - 3) {
+        float w = vy[i];
+        if (__ldg(cy + i) & FC_M) w = w - ih * (float)(__ldg(xv + i + P) - __ldg(xv + i));
+        vy[i] = w;
+        m = fmaxf(m, fabsf(w));
+      }
+    }
+  }
+  if (umax_bits) {
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float red[BY];
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    if ((tid & 31) == 0) red[tid >> 5] = m;
+    __syncthreads();
+    if (tid == 0) {
+      for (int k = 1; k < BY; k++) m = fmaxf(m, red[k]);
+      atomicMax(umax_bits, __float_as_uint(m));
+    }
+  }
+}
+
+size_t a256(size_t v) { return (v + 255) / 256 * 256; }
+
+}  // namespace
+
+void fcg_alloc(FcgSolver &fs, int W, int H, int P, float h) {
+  fcg_free(fs);
+  ext_hier_alloc(fs.mg, W, H, h);
+  size_t n = (size_t)P * H;
+  size_t total = a256(sizeof(FcgScalars)) + a256(n * 8) + 3 * a256(n * 4);
+  void *arena = nullptr;
+  if (cudaMalloc(&arena, total) != cudaSuccess) {
+    cudaGetLastError();
+    fcg_free(fs);
+    throw std::bad_alloc();
+  }
+  UBG_CUDA(cudaMemsetAsync(arena, 0, total, cudaStreamLegacy));
+  UBG_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
+  void *host = nullptr;
+  if (cudaHostAlloc(&host, sizeof(FcgScalars), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(arena);
+    fcg_free(fs);
+    throw std::bad_alloc();
+  }
+  char *p = (char *)arena;
+  fs.dev = (FcgScalars *)p;
+  p += a256(sizeof(FcgScalars));
+  fs.x = (double *)p;
+  p += a256(n * 8);
+  fs.d[0] = (float *)p;
+  p += a256(n * 4);
+  fs.d[1] = (float *)p;
+  p += a256(n * 4);
+  fs.q = (float *)p;
+  fs.arena = arena;
+  fs.host = (FcgScalars *)host;
+  fs.W = W;
+  fs.H = H;
+  fs.P = P;
+  fs.h = h;
+  fs.dirty = true;
+  fs.prec = UBG_FP32;
+}
+
+void fcg_free(FcgSolver &fs) {
+  mg_low_free(fs.lo);
+  mg_free(fs.mg);
+  fs.mg = MgHier{};
+  if (fs.arena) cudaFree(fs.arena);
+  if (fs.host) cudaFreeHost(fs.host);
+  fs.arena = nullptr;
+  fs.host = nullptr;
+  fs.dev = nullptr;
+  fs.x = nullptr;
+  fs.d[0] = fs.d[1] = fs.q = nullptr;
+}
+
+size_t fcg_bytes(int W, int H, int P, int prec) {
+  size_t n = (size_t)P * H;
+  size_t b = ext_hier_bytes(W, H) + a256(sizeof(FcgScalars)) + a256(n * 8) + 3 * a256(n * 4);
+  if (prec != UBG_FP32) b += b / 2;  // 16-bit copies of the hierarchy's arrays (upper bound)
+  return b;
+}
+
+void fcg_set_precision(FcgSolver &fs, int prec) {
+  if (prec == fs.prec && (prec == UBG_FP32 || fs.lo.levels == fs.mg.levels)) return;
+  if (prec == UBG_FP32)
+    mg_low_free(fs.lo);
+  else
+    mg_low_alloc(fs.lo, fs.mg, prec);
+  fs.prec = prec;
+}
+
+int fcg_solve(FcgSolver &fs, const uint8_t *flag, const float *f, float *p, double tol,
+              int max_iter, double *rel, cudaStream_t st) {
+  const int W = fs.W, H = fs.H, P = fs.P;
+  MgHier &mg = fs.mg;
+  MgLevel &L0 = mg.lv[0];
+  if (fs.dirty) {
+    ext_hier_update_fields(mg, flag, P, st);
+    fs.dirty = false;
+  }
+  const float ihsq = 1.0f / fs.h / fs.h;
+  const dim3 grid((W + 4 * BX - 1) / (4 * BX), (H + BY - 1) / BY), blk(BX, BY);
+  float *r = L0.rhs;  // the V-cycle's level-0 right-hand side is the residual
+  UBG_CUDA(cudaMemsetAsync(fs.dev, 0, sizeof(FcgScalars), st));
+  k_fcg_load<<<grid, blk, 0, st>>>(p, fs.x, W, H, P);
+  UBG_LAUNCH_CHECK();
+  k_fcg_fsum<<<grid, blk, 0, st>>>(f, L0.code, W, H, P, fs.dev);
+  UBG_LAUNCH_CHECK();
+  k_fcg_resid<<<grid, blk, 0, st>>>(fs.x, f, L0.code, W, H, P, ihsq, r, fs.dev, 1);
+  UBG_LAUNCH_CHECK();
+  g_stats.launches += 3;
+  auto read = [&]() {
+    UBG_CUDA(cudaMemcpyAsync(fs.host, fs.dev, sizeof(FcgScalars), cudaMemcpyDeviceToHost, st));
+    UBG_CUDA(cudaStreamSynchronize(st));
+  };
+  read();
+  const double ff = fs.host->ff, target2 = tol * tol * ff;
+  // The recurrence r -= alpha q drifts from f_c + L x by FP32 rounding; when
+  // it meets the tolerance, r is recomputed from x (residual replacement)
+  // and, if that misses the tolerance, the iteration restarts from it.  A
+  // replacement that finds the residual not at least halved since the last
+  // one ends the solve: the tolerance is below what the FP32 vectors
+  // resolve.
+  double rr = fs.host->rr, last_true = rr;
+  bool fresh = true, first = true;
+  int it = 0, cur_d = 0;
+  auto replace_residual = [&]() {
+    UBG_CUDA(cudaMemsetAsync(&fs.dev->rr, 0, sizeof(double), st));
+    UBG_CUDA(cudaMemsetAsync(&fs.dev->maxbits, 0, sizeof(unsigned), st));
+    k_fcg_resid<<<grid, blk, 0, st>>>(fs.x, f, L0.code, W, H, P, ihsq, r, fs.dev, 0);
+    UBG_LAUNCH_CHECK();
+    g_stats.launches++;
+    read();
+    rr = fs.host->rr;
+    fresh = true;
+    first = true;
+  };
+  for (;;) {
+    if (!std::isfinite(rr)) throw CudaError("tolerance solver: non-finite residual");
+    if (rr <= target2) {
+      if (fresh) break;
+      replace_residual();
+      if (rr > 0.25 * last_true) break;
+      last_true = rr;
+      continue;
+    }
+    if (it >= max_iter) {
+      if (!fresh) replace_residual();
+      break;
+    }
+    ext_vcycle(mg, fs.prec == UBG_FP32 ? nullptr : &fs.lo, fs.prec, &fs.dev->maxbits, st);
+    const float *z = L0.e[mg.cur0];
+    const int slot = it & 1;
+    if (it > 0) {  // (also zeroes the accumulators of k_fcg_dir)
+      k_fcg_zq<<<grid, blk, 0, st>>>(z, fs.q, W, H, P, fs.dev, slot);
+      UBG_LAUNCH_CHECK();
+      g_stats.launches++;
+    }
+    k_fcg_dir<<<grid, blk, 0, st>>>(z, fs.d[cur_d], fs.d[cur_d ^ 1], fs.q, r, L0.code, W, H, P,
+                                    ihsq, fs.dev, first ? 1 : 0, slot);
+    UBG_LAUNCH_CHECK();
+    cur_d ^= 1;
+    k_fcg_update<<<grid, blk, 0, st>>>(fs.x, fs.d[cur_d], r, fs.q, W, H, P, fs.dev, slot);
+    UBG_LAUNCH_CHECK();
+    g_stats.launches += 2;
+    it++;
+    first = false;
+    fresh = false;
+    read();
+    rr = fs.host->rr;
+  }
+  k_fcg_store<<<grid, blk, 0, st>>>(fs.x, p, W, H, P);
+  UBG_LAUNCH_CHECK();
+  g_stats.launches++;
+  if (rel) *rel = std::sqrt(rr / (ff > 0.0 ? ff : 1.0));
+  return it;
+}
+
+void launch_gradient64(const VelBufs &v, int fx, int fy, const double *x, const StepScalars *sc,
+                       unsigned *umax_bits, cudaStream_t st) {
+  ProfScope ps_(KC_GRADIENT, st);
+  const dim3 grid((v.W + 4 * BX - 1) / (4 * BX), (v.H + BY - 1) / BY);
+  k_gradient64<<<grid, dim3(BX, BY), 0, st>>>(fx ? v.vx[1] : v.vx[0], fy ? v.vy[1] : v.vy[0], v.cx,
+                                               v.cy, x, v.W, v.H, v.pitch, sc, umax_bits);
+  UBG_LAUNCH_CHECK();
+  g_stats.launches++;
+}
+
+}  // namespace ubg

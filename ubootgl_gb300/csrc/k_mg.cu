@@ -209,7 +209,9 @@ struct Sto<__nv_bfloat16> {
   }
 };
 
-template <class S>
+// S: storage of the level's own arrays (in, out, rhs); SC: storage of the
+// next coarser level's arrays that the launch reads (ec) or writes (rc).
+template <class S, class SC = S>
 struct MgArgsT {
   const S *in;
   S *out;
@@ -219,20 +221,47 @@ struct MgArgsT {
   float hh, alpha, ihsq;
   int nsweeps, zgbc, zero_init;
   // prologue: p += prolongate(ec) (post-smoothing)
-  const S *ec;
+  const SC *ec;
   const uint8_t *codec;
   int cpitch;
   float wsum[5];   // (float)((double)k + 0.0001)
   float rwsum[5];  // RN(1 / wsum[k]), for div_rn
   // epilogue: rc = restrict(residual) (pre-smoothing)
-  S *rc;
+  SC *rc;
   int cw, ch;
   float rfac;  // restriction weight: 1/16 (reference), 1/16 * (hc/h)^2 (scaled form)
   int tile;    // smoother tile id (-1: by level width), host side only
   // epilogue: sum of r^2 over the tile's interior cells
   double *norm2;
+  // Tolerance-solver hierarchy (ext != 0): zero-gradient edges on every
+  // level include the four corner cells, and the prolongation has no
+  // zero columns / rows at the east and north ends (the coarse edges there
+  // are zero-gradient copies, not zeros).
+  int ext;
+  // Scaled 16-bit coarse levels below an FP32 level (scale_bits != null):
+  // s = 2^-(e + scale_kexp) with max|rhs| * scale_h1sq = m 2^e, m in
+  // [0.5, 1) (max|rhs| as float bits on the device); the restriction
+  // writes rfac * s * scale_h1sq * (...) and the prolongation adds e_c / s.
+  const unsigned *scale_bits;
+  float scale_h1sq;
+  int scale_kexp;
 };
 using MgArgs = MgArgsT<float>;
+
+// Scale of the 16-bit coarse levels from max|r| (float bits): returns s and
+// sets *inv = 1 / s (both powers of two; 0 when r is zero).
+__device__ __forceinline__ float coarse_scale(const unsigned *bits, float h1sq, int kexp,
+                                              float *inv) {
+  const float m = __uint_as_float(*bits) * h1sq;
+  if (!(m > 0.0f)) {
+    *inv = 0.0f;
+    return 0.0f;
+  }
+  int ex;
+  frexpf(m, &ex);
+  *inv = ldexpf(1.0f, ex + kexp);
+  return ldexpf(1.0f, -ex - kexp);
+}
 
 template <int TX, int TY, int HALO>
 struct Tile {
@@ -242,10 +271,10 @@ struct Tile {
   static constexpr int CW = HX + 4, CH = RY / 2 + 2;
   static_assert(RX % 4 == 0 && HALO % 4 == 0 && TX % 4 == 0 && TY % 2 == 0, "tile alignment");
   // shared memory for element size ES: p and f in the split layout, codes,
-  // the coarse window (values and flags)
-  static constexpr size_t smem(size_t ES = 4) {
-    return (size_t)2 * RY * HX * (2 * ES + 1) + (((size_t)CW * CH * ES + 15) / 16 * 16) +
-           ((size_t)CW * CH + 15) / 16 * 16;
+  // the coarse window (values of element size ESC, and flags)
+  static constexpr size_t smem(size_t ES = 4, size_t ESC = 0) {
+    return (size_t)2 * RY * HX * (2 * ES + 1) +
+           (((size_t)CW * CH * (ESC ? ESC : ES) + 15) / 16 * 16) + ((size_t)CW * CH + 15) / 16 * 16;
   }
 };
 
@@ -256,11 +285,12 @@ struct Tile {
 // (no bank conflicts).  Red = (x+y) odd; region parity equals global parity
 // because x0 + y0 is even.  After half sweep i only cells within HALO - i of
 // the tile are still exact, so each half sweep updates just that cone.
-template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S>
-__device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, const int by) {
+template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S, class SC>
+__device__ __forceinline__ void k_mg_body(const MgArgsT<S, SC> &a, const int bx, const int by) {
   constexpr int NTY = NT / 32;
   using T = Tile<TX, TY, HALO>;
   using St = Sto<S>;
+  using Sc = Sto<SC>;
   constexpr int RX = T::RX, RY = T::RY, HX = T::HX;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S *sp = reinterpret_cast<S *>(smem_raw);  // [2][RY][HX]
@@ -342,9 +372,9 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
     // while the code loads are in flight, stored before the same barrier
     if (a.ec) {
       constexpr int CW = T::CW, CH = T::CH;
-      S *sec = reinterpret_cast<S *>(sc + 2 * RY * HX);
+      SC *sec = reinterpret_cast<SC *>(sc + 2 * RY * HX);
       uint8_t *scf = reinterpret_cast<uint8_t *>(sc + 2 * RY * HX) +
-                     ((size_t)CW * CH * sizeof(S) + 15) / 16 * 16;
+                     ((size_t)CW * CH * sizeof(SC) + 15) / 16 * 16;
       const int cxa = x0 >> 1, cya = y0 >> 1;
       // all of a thread's loads in flight together, then the stores
       if constexpr (HALO % 8 == 0) {
@@ -361,7 +391,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
           ev[it] = make_float4(0.f, 0.f, 0.f, 0.f);
           fv[it] = 0u;
           if (q < CQ4 && cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
-            ev[it] = St::ldg4(a.ec + (size_t)cy * a.cpitch + cx);
+            ev[it] = Sc::ldg4(a.ec + (size_t)cy * a.cpitch + cx);
             fv[it] = __ldg(reinterpret_cast<const unsigned *>(a.codec + (size_t)cy * a.cpitch + cx)) &
                      0x01010101u;
             if (cx + 3 >= a.cw) {  // entries at and beyond the level's width are 0
@@ -376,7 +406,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
         for (int it = 0; it < CIT; it++) {
           const int q = tid + it * NT;
           if (q < CQ4) {
-            St::sts4(sec + 4 * q, ev[it]);
+            Sc::sts4(sec + 4 * q, ev[it]);
             *reinterpret_cast<unsigned *>(scf + 4 * q) = fv[it];
           }
         }
@@ -392,7 +422,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
           ev[it] = 0.0f;
           fv[it] = 0;
           if (q < CQ && cx >= 0 && cx < a.cw && cy >= 0 && cy < a.ch) {
-            ev[it] = St::ldg1(a.ec + (size_t)cy * a.cpitch + cx);
+            ev[it] = Sc::ldg1(a.ec + (size_t)cy * a.cpitch + cx);
             fv[it] = __ldg(a.codec + (size_t)cy * a.cpitch + cx) & 1u;
           }
         }
@@ -400,7 +430,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
         for (int it = 0; it < CIT; it++) {
           int q = tid + it * NT;
           if (q < CQ) {
-            sec[q] = St::fromf(ev[it]);
+            sec[q] = Sc::fromf(ev[it]);
             scf[q] = fv[it];
           }
         }
@@ -460,9 +490,13 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   // the coarse window staged with the field loads above
   if (a.ec) {
     constexpr int CW = T::CW, CH = T::CH;
-    S *sec = reinterpret_cast<S *>(sc + 2 * RY * HX);
+    SC *sec = reinterpret_cast<SC *>(sc + 2 * RY * HX);
     uint8_t *scf = reinterpret_cast<uint8_t *>(sc + 2 * RY * HX) +
-                   ((size_t)CW * CH * sizeof(S) + 15) / 16 * 16;
+                   ((size_t)CW * CH * sizeof(SC) + 15) / 16 * 16;
+    // correction scale of scaled 16-bit coarse levels (1 otherwise)
+    float ecmul = 1.0f;
+    if (a.scale_bits) coarse_scale(a.scale_bits, a.scale_h1sq, a.scale_kexp, &ecmul);
+    const bool ext = a.ext != 0;
     // prolongate (pressure_solver.cpp:134-172); e * fine flag = e here.
     // Fine cell (rx, ry) = (2k + par, ry) lies over coarse column k of the
     // window and coarse row ry / 2; x parity is par and y parity ry & 1, both
@@ -477,20 +511,20 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
         const unsigned cw4 = *reinterpret_cast<const unsigned *>(sc + row);
         if ((cw4 & 0x01010101u) == 0u) continue;  // no fluid cell among the 4
         const int eo = (ry >> 1) * CW + k0w;
-        const float4 ea = St::lds4(sec + eo);
-        const float E0[5] = {ea.x, ea.y, ea.z, ea.w, St::tof(sec[eo + 4])};
+        const float4 ea = Sc::lds4(sec + eo);
+        const float E0[5] = {ea.x, ea.y, ea.z, ea.w, Sc::tof(sec[eo + 4])};
         const unsigned fa = *reinterpret_cast<const unsigned *>(scf + eo);
         const unsigned F0[5] = {fa & 0xffu, (fa >> 8) & 0xffu, (fa >> 16) & 0xffu, fa >> 24,
                                 scf[eo + 4]};
         float E1[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
         unsigned F1[5] = {0u, 0u, 0u, 0u, 0u};
         if (yo) {
-          const float4 eb = St::lds4(sec + eo + CW);
+          const float4 eb = Sc::lds4(sec + eo + CW);
           E1[0] = eb.x;
           E1[1] = eb.y;
           E1[2] = eb.z;
           E1[3] = eb.w;
-          E1[4] = St::tof(sec[eo + CW + 4]);
+          E1[4] = Sc::tof(sec[eo + CW + 4]);
           const unsigned fb = *reinterpret_cast<const unsigned *>(scf + eo + CW);
           F1[0] = fb & 0xffu;
           F1[1] = (fb >> 8) & 0xffu;
@@ -509,16 +543,17 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
             pe = E0[j];
           } else if (par && !yo) {
             const int k = F0[j] + F0[j + 1];
-            pe = (gx >= w - 2) ? 0.0f : div_rn(E0[j] + E0[j + 1], a.wsum[k], a.rwsum[k]);
+            pe = (!ext && gx >= w - 2) ? 0.0f : div_rn(E0[j] + E0[j + 1], a.wsum[k], a.rwsum[k]);
           } else if (!par && yo) {
             const int k = F0[j] + F1[j];
-            pe = (gy >= h - 2) ? 0.0f : div_rn(E0[j] + E1[j], a.wsum[k], a.rwsum[k]);
+            pe = (!ext && gy >= h - 2) ? 0.0f : div_rn(E0[j] + E1[j], a.wsum[k], a.rwsum[k]);
           } else {
             const int k = F0[j] + F1[j + 1] + F0[j + 1] + F1[j];
-            pe = (gx >= w - 2 || gy >= h - 2)
+            pe = (!ext && (gx >= w - 2 || gy >= h - 2))
                      ? 0.0f
                      : div_rn(((E0[j] + E1[j + 1]) + E0[j + 1]) + E1[j], a.wsum[k], a.rwsum[k]);
           }
+          if (a.scale_bits) pe = pe * ecmul;
           out[j] = out[j] + pe;
         }
         St::sts4(sp + row, make_float4(out[0], out[1], out[2], out[3]));
@@ -547,6 +582,14 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
       int rn = side ? ry - 1 : ry + 1;
       if (ry < 0 || ry >= RY || rn < 0 || rn >= RY) continue;
       sp[IDX(rx, ry)] = sp[IDX(rx, rn)];
+    }
+    if (a.ext && tid < 4) {  // corner cell <- its diagonal interior neighbour
+      const int cxg = (tid & 1) ? w - 1 : 0, cyg = (tid & 2) ? h - 1 : 0;
+      const int rx = cxg - x0, ry = cyg - y0;
+      const int rnx = rx + ((tid & 1) ? -1 : 1), rny = ry + ((tid & 2) ? -1 : 1);
+      if (rx >= 0 && rx < RX && ry >= 0 && ry < RY && rnx >= 0 && rnx < RX && rny >= 0 &&
+          rny < RY)
+        sp[IDX(rx, ry)] = sp[IDX(rnx, rny)];
     }
   };
   if (a.zgbc && edge && a.ec) {
@@ -732,13 +775,18 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
   // ---- restrict (pressure_solver.cpp:118-132) onto the coarse tile -------
   if (a.rc) {
     const int cx0 = bx * (TX / 2), cy0 = by * (TY / 2);
+    float rfac = a.rfac;
+    if (a.scale_bits) {
+      float inv;
+      rfac = rfac * (coarse_scale(a.scale_bits, a.scale_h1sq, a.scale_kexp, &inv) * a.scale_h1sq);
+    }
     // one coarse cell: full weighting of the 3x3 fine residuals around it
     auto restrict1 = [&](float m1, float c0, float p1, float m2, float c2, float p2, float m3,
                          float c3, float p3) {
       float v = (m1 * 1.0f + c0 * 2.0f) + p1 * 1.0f;
       v = v + ((m2 * 2.0f + c2 * 4.0f) + p2 * 2.0f);
       v = v + ((m3 * 1.0f + c3 * 2.0f) + p3 * 1.0f);
-      return v * a.rfac;
+      return v * rfac;
     };
     if constexpr (HALO % 8 == 0 && (TX / 2) % 4 == 0) {
       // 4 consecutive coarse cells per thread.  Coarse column X sits over
@@ -776,13 +824,13 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
             v[j] = restrict1(oth[0][j], cen[0][j], oth[0][j + 1], oth[1][j], cen[1][j],
                              oth[1][j + 1], oth[2][j], cen[2][j], oth[2][j + 1]);
         }
-        S *dst = a.rc + (size_t)Y * a.cpitch + X0;
+        SC *dst = a.rc + (size_t)Y * a.cpitch + X0;
         if (X0 + 3 < a.cw) {
-          St::st4(dst, make_float4(v[0], v[1], v[2], v[3]));
+          Sc::st4(dst, make_float4(v[0], v[1], v[2], v[3]));
         } else {
 #pragma unroll
           for (int j = 0; j < 4; j++)
-            if (X0 + j < a.cw) dst[j] = St::fromf(v[j]);
+            if (X0 + j < a.cw) dst[j] = Sc::fromf(v[j]);
         }
       }
     } else {
@@ -797,16 +845,17 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S> &a, const int bx, con
           v = restrict1(R(-1, -1), R(0, -1), R(1, -1), R(-1, 0), R(0, 0), R(1, 0), R(-1, 1),
                         R(0, 1), R(1, 1));
         }
-        a.rc[(size_t)Y * a.cpitch + X] = St::fromf(v);
+        a.rc[(size_t)Y * a.cpitch + X] = Sc::fromf(v);
       }
     }
   }
 }
 
-template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float>
-__global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4)) k_mg(MgArgsT<S> a) {
+template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float, class SC = S>
+__global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4))
+    k_mg(MgArgsT<S, SC> a) {
   griddep_wait();
-  k_mg_body<TX, TY, HALO, ALPHA1, NT, S>(a, blockIdx.x, blockIdx.y);
+  k_mg_body<TX, TY, HALO, ALPHA1, NT, S, SC>(a, blockIdx.x, blockIdx.y);
 }
 // One launch over the members of a batch (FP32): block -> member -> tile.
 template <int TX, int TY, int HALO, bool ALPHA1, int NT>
@@ -818,7 +867,7 @@ __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4))
   const int m = member_of(bs, n);
   const MgArgs &a = A[m];
   const int l = (int)blockIdx.x - __ldg(bs + m), gx = (a.w + TX - 1) / TX;
-  k_mg_body<TX, TY, HALO, ALPHA1, NT, float>(a, l % gx, l / gx);
+  k_mg_body<TX, TY, HALO, ALPHA1, NT, float, float>(a, l % gx, l / gx);
 }
 
 // ------------------------------------------------------ residual field only
@@ -908,6 +957,11 @@ struct TailArgs {
   int float_words;  // elements of the arithmetic part of shared memory
   float wsum[5];
   float rwsum[5];  // RN(1 / wsum[k])
+  // Tolerance-solver hierarchy: zero-gradient edges (corners included) on
+  // every level after every sweep and after the correction, no zero
+  // columns / rows in the prolongation, `ncoarse` sweeps on the coarsest
+  // level (the last one of the tail) instead of 5.
+  int ext, ncoarse;
 };
 
 // A level may be worked by a team of threads (a prefix of the block, with
@@ -963,6 +1017,34 @@ __device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
   }
   __syncthreads();
 
+  // setZeroGradientBC on level t, plus the corners in ext mode
+  auto zero_gradient = [&](int t, int team) {
+    const TailLevel &L = a.L[t];
+    T *e = fm + L.oe;
+    const int w = L.w, hh2 = L.h, ny = hh2 - 2, nx = w - 2;
+    for (int q = tid; q < 2 * ny + 2 * nx + 4; q += team) {
+      if (q < 2 * ny) {
+        const int y = 1 + (q >> 1);
+        if (q & 1)
+          e[y * w + w - 1] = e[y * w + w - 2];
+        else
+          e[y * w] = e[y * w + 1];
+      } else if (q < 2 * ny + 2 * nx) {
+        const int k = q - 2 * ny, x = 1 + (k >> 1);
+        if (k & 1)
+          e[(hh2 - 1) * w + x] = e[(hh2 - 2) * w + x];
+        else
+          e[x] = e[w + x];
+      } else {
+        const int c = q - 2 * ny - 2 * nx;
+        const int cx = (c & 1) ? w - 1 : 0, cy = (c & 2) ? hh2 - 1 : 0;
+        const int nxx = (c & 1) ? w - 2 : 1, nyy = (c & 2) ? hh2 - 2 : 1;
+        e[cy * w + cx] = e[nyy * w + nxx];
+      }
+    }
+    team_sync(team);
+  };
+
   auto sweeps = [&](int t, int ns, int team) {
     const TailLevel &L = a.L[t];
     T *e = fm + L.oe;
@@ -988,6 +1070,7 @@ __device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
         }
         team_sync(team);
       }
+      if (a.ext) zero_gradient(t, team);
     }
   };
 
@@ -997,7 +1080,7 @@ __device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
     if (tid >= team) continue;
     const int ystep = team / 32;
     if (t == nl - 1) {
-      sweeps(t, 5, team);
+      sweeps(t, a.ext ? a.ncoarse : 5, team);
       break;
     }
     sweeps(t, 3, team);
@@ -1048,21 +1131,25 @@ __device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
         auto E = [&](int xx, int yy) { return ec[yy * C.w + xx]; };
         auto F = [&](int xx, int yy) { return (int)(cc[yy * C.w + xx] & 1u); };
         bool xo = x & 1, yo = y & 1;
+        const bool ext = a.ext != 0;
         T ev;
         if (!xo && !yo)
           ev = E(cx, cy);
         else if (xo && !yo)
-          ev = (x >= L.w - 2) ? T(0) : DIVW(E(cx, cy) + E(cx + 1, cy), F(cx, cy) + F(cx + 1, cy));
+          ev = (!ext && x >= L.w - 2) ? T(0)
+                                      : DIVW(E(cx, cy) + E(cx + 1, cy), F(cx, cy) + F(cx + 1, cy));
         else if (!xo && yo)
-          ev = (y >= L.h - 2) ? T(0) : DIVW(E(cx, cy) + E(cx, cy + 1), F(cx, cy) + F(cx, cy + 1));
+          ev = (!ext && y >= L.h - 2) ? T(0)
+                                      : DIVW(E(cx, cy) + E(cx, cy + 1), F(cx, cy) + F(cx, cy + 1));
         else
-          ev = (x >= L.w - 2 || y >= L.h - 2)
+          ev = (!ext && (x >= L.w - 2 || y >= L.h - 2))
                    ? T(0)
                    : DIVW(((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1),
                           F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1));
         e[q] = e[q] + ev;
       }
     team_sync(team);
+    if (a.ext) zero_gradient(t, team);
     sweeps(t, 3, team);
   }
   __syncthreads();
@@ -1087,23 +1174,24 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1)
 }
 
 // ------------------------------------------------------------ launches
-template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float>
-void launch_mg_t(const MgArgsT<S> &a, cudaStream_t st) {
+template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float, class SC = S>
+void launch_mg_t(const MgArgsT<S, SC> &a, cudaStream_t st) {
   using T = Tile<TX, TY, HALO>;
   dim3 grid((a.w + TX - 1) / TX, (a.h + TY - 1) / TY);
-  launch_pdl(k_mg<TX, TY, HALO, A1, NT, S>, grid, dim3(32, NT / 32), T::smem(sizeof(S)), st, a);
+  launch_pdl(k_mg<TX, TY, HALO, A1, NT, S, SC>, grid, dim3(32, NT / 32),
+             T::smem(sizeof(S), sizeof(SC)), st, a);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
 
-template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float>
+template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float, class SC = S>
 void set_smem_attr() {
-  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S>,
+  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S, SC>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)Tile<TX, TY, HALO>::smem(sizeof(S))));
+                                (int)Tile<TX, TY, HALO>::smem(sizeof(S), sizeof(SC))));
   // one carveout for every kernel of a V-cycle: no L1 / shared-memory
   // reconfiguration between consecutive launches
-  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S>,
+  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S, SC>,
                                 cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 }
 
@@ -1154,6 +1242,14 @@ static void set_all_kernel_attributes() {
   set_vcycle_attrs<__nv_bfloat16>();
   set_tail_attr<__half, double>();
   set_tail_attr<__nv_bfloat16, double>();
+  // the tolerance solver: FP32 level 0 over 16-bit coarse levels, FP32
+  // arithmetic in the tail over 16-bit storage
+  set_smem_attr<112, 50, 8, true, 512, float, __half>();
+  set_smem_attr<48, 16, 8, true, 256, float, __half>();
+  set_smem_attr<112, 50, 8, true, 512, float, __nv_bfloat16>();
+  set_smem_attr<48, 16, 8, true, 256, float, __nv_bfloat16>();
+  set_tail_attr<__half, float>();
+  set_tail_attr<__nv_bfloat16, float>();
 }
 
 void init_kernel_attributes() {
@@ -1181,6 +1277,18 @@ void launch_mg_tile(const MgArgsT<S> &a, int id, cudaStream_t st) {
     case 5: launch_mg_t<112, 114, 8, true, 1024, S>(a, st); break;
     default: throw ArgError("smoother tile id");
   }
+}
+
+// An FP32 level over 16-bit coarse arrays (the tolerance solver's level 0):
+// 3 sweeps, tile by level width.
+template <class SC>
+void launch_mg_mixed_top(const MgArgsT<float, SC> &a, cudaStream_t st) {
+  if (!ALPHA_IS_ONE(a.alpha) || a.nsweeps < 1 || a.nsweeps > 3)
+    throw ArgError("mixed top level: alpha = 1, at most 3 sweeps");
+  if (a.w >= 1200)
+    launch_mg_t<112, 50, 8, true, 512, float, SC>(a, st);
+  else
+    launch_mg_t<48, 16, 8, true, 256, float, SC>(a, st);
 }
 
 template <class S>
@@ -1230,11 +1338,13 @@ MgArgs level_args(MgLevel &L, const float *in, float *out, int ns, float alpha) 
   return a;
 }
 
-// Shared-memory bytes of the tail for levels lt .. levels-2 with arithmetic
-// type of elem_bytes.
-size_t tail_smem_bytes(const std::vector<MgLevel> &lv, int lt, size_t elem_bytes) {
+// Shared-memory bytes of the tail for levels lt .. last (default
+// levels-2, the reference's coarsest level) with arithmetic type of
+// elem_bytes.
+size_t tail_smem_bytes(const std::vector<MgLevel> &lv, int lt, size_t elem_bytes, int last = -1) {
   size_t fw = 0, bw = 0;
-  for (int t = lt; t <= (int)lv.size() - 2; t++) {
+  if (last < 0) last = (int)lv.size() - 2;
+  for (int t = lt; t <= last; t++) {
     size_t n = (size_t)lv[t].w * lv[t].h;
     fw += 3 * ((n + 3) / 4 * 4);
     bw += (n + 15) / 16 * 16;
@@ -1248,8 +1358,10 @@ template <class S, class T>
 TailArgs<S> tail_args(MgHier &mg, int lt, const S *rhs_top, S *e_top, const float *rfac,
                       size_t *smem_out) {
   TailArgs<S> a{};
-  int nl = mg.levels - 1 - lt;
+  int nl = mg_coarsest(mg) + 1 - lt;
   a.nlev = nl;
+  a.ext = mg.ext ? 1 : 0;
+  a.ncoarse = mg.ncoarse;
   size_t fw = 0, bw = 0;
   for (int t = 0; t < nl; t++) {
     MgLevel &L = mg.lv[lt + t];
@@ -1692,10 +1804,12 @@ size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 // The first level whose whole coarse end fits the tail kernel (arithmetic
 // elements of elem_bytes: 4 for FP32, 8 for the mixed solver's FP64) with a
 // top level of at most max_cells.
-int choose_tail(const std::vector<MgLevel> &lv, int max_cells, size_t elem_bytes = 4) {
+int choose_tail(const std::vector<MgLevel> &lv, int max_cells, size_t elem_bytes = 4,
+                int last = -1) {
   int L = (int)lv.size();
-  for (int lt = 1; lt <= L - 2; lt++) {
-    if (tail_smem_bytes(lv, lt, elem_bytes) <= TAIL_SMEM_MAX &&
+  if (last < 0) last = L - 2;
+  for (int lt = 1; lt <= last; lt++) {
+    if (tail_smem_bytes(lv, lt, elem_bytes, last) <= TAIL_SMEM_MAX &&
         (size_t)lv[lt].w * lv[lt].h <= (size_t)max_cells)
       return lt;
   }
@@ -2186,6 +2300,282 @@ void level_residual(const MgLevel &L, int cur, float *r, double *norm2, cudaStre
                                            norm2);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
+}
+
+
+// ------------------------------------------- tolerance-solver hierarchy
+// The tolerance solver (k_krylov.cu) preconditions its Krylov loop with a
+// V-cycle of its own hierarchy, built for convergence rather than for
+// parity with MG::solveLevel:
+//  * level sizes floor(w/2)+1, so coarse cell X sits over fine cell 2X for
+//    every interior fine cell up to the last one and coarse edges sit over
+//    fine edges (the reference's floor(w/2) leaves the last fine columns
+//    and rows without a coarse cell);
+//  * spacing doubles exactly per level;
+//  * a coarse cell is fluid if any of the nine fine cells of its
+//    full-weighting stencil is (the reference keeps it only above a
+//    weighted fraction of 0.2, which closes narrow gaps on coarse levels);
+//    coarse edge cells are fluid, as in the reference;
+//  * zero-gradient edges (corners included) on every level, so every level
+//    solves the zero-gradient system; no zero columns / rows in the
+//    prolongation;
+//  * the last level is the coarsest, with 40 sweeps.
+namespace {
+std::vector<MgLevel> ext_shapes(int W, int H, float h0) {
+  std::vector<MgLevel> lv;
+  int w = W, h = H;
+  float hh = h0;
+  for (;;) {
+    MgLevel L{};
+    L.w = w;
+    L.h = h;
+    L.pitch = round_up(w, 32);
+    L.hh = hh;
+    lv.push_back(L);
+    const int nw = w / 2 + 1, nh = h / 2 + 1;
+    if (nw < 5 || nh < 5 || nw >= w || nh >= h) break;
+    w = nw;
+    h = nh;
+    hh = 2.0f * hh;
+  }
+  if (lv.size() < 2) throw ArgError("grid too small for the tolerance solver (need W, H >= 8)");
+  return lv;
+}
+
+// Coarse flags of the tolerance hierarchy: interior cell (X, Y) is fluid if
+// any fine cell (2X + dx, 2Y + dy), |dx|, |dy| <= 1, is; edge cells are 1.
+__global__ void k_coarsen_ext(const uint8_t *__restrict__ f, int fp, uint8_t *fc, int cw, int ch,
+                              int cp) {
+  const int X = blockIdx.x * 32 + threadIdx.x, Y = blockIdx.y * 8 + threadIdx.y;
+  if (X >= cw || Y >= ch) return;
+  uint8_t v = 1;
+  if (X >= 1 && X < cw - 1 && Y >= 1 && Y < ch - 1) {
+    unsigned any = 0;
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+      for (int dx = -1; dx <= 1; dx++) any |= __ldg(f + (size_t)(2 * Y + dy) * fp + 2 * X + dx);
+    v = any ? 1 : 0;
+  }
+  fc[(size_t)Y * cp + X] = v;
+}
+
+template <class S>
+void ext_fill_common(MgArgsT<S> &a) {
+  for (int k = 0; k < 5; k++) {
+    a.wsum[k] = (float)((double)(float)k + 0.0001);
+    a.rwsum[k] = 1.0f / a.wsum[k];
+  }
+  a.alpha = 1.0f;
+  a.tile = -1;
+  a.ext = 1;
+  a.zgbc = 1;
+}
+
+// Level l >= 1 of the tolerance hierarchy: FP32 arrays of mg (unscaled
+// form) or the 16-bit arrays of lo (h^2-scaled form: hh = 1, restriction
+// weight (1/16) (h_c / h)^2 = 1/4 because the spacing doubles).
+template <class SC>
+MgArgsT<SC> ext_level_args(MgHier &mg, MgLow *lo, int l, int cin, int ns) {
+  constexpr bool scaled = !std::is_same<SC, float>::value;
+  MgLevel &L = mg.lv[l];
+  MgArgsT<SC> a{};
+  if (scaled) {
+    a.in = (const SC *)lo->e[cin][l];
+    a.out = (SC *)lo->e[1 - cin][l];
+    a.rhs = (const SC *)lo->rhs[l];
+  } else {
+    a.in = (const SC *)L.e[cin];
+    a.out = (SC *)L.e[1 - cin];
+    a.rhs = (const SC *)L.rhs;
+  }
+  a.code = L.code;
+  a.w = L.w;
+  a.h = L.h;
+  a.pitch = L.pitch;
+  a.hh = scaled ? 1.0f : L.hh;
+  a.ihsq = scaled ? 1.0f : 1.0f / L.hh / L.hh;
+  a.nsweeps = ns;
+  a.rfac = scaled ? 0.25f : 1.0f / 16.0f;
+  ext_fill_common(a);
+  return a;
+}
+
+template <class SC>
+void ext_vcycle_t(MgHier &mg, MgLow *lo, const unsigned *scale_bits, cudaStream_t st) {
+  constexpr bool scaled = !std::is_same<SC, float>::value;
+  const int T = mg.tail_top;
+  if (T < 1) throw ArgError("tolerance hierarchy without a coarse tail");
+  auto arr = [&](int l, int c) -> SC * {
+    return scaled ? (SC *)lo->e[c][l] : (SC *)mg.lv[l].e[c];
+  };
+  auto rhs = [&](int l) -> SC * { return scaled ? (SC *)lo->rhs[l] : (SC *)mg.lv[l].rhs; };
+  std::vector<int> cur(mg.levels, 0);
+  MgLevel &L0 = mg.lv[0], &L1 = mg.lv[1];
+  int kexp = 0;
+  if (std::is_same<SC, __half>::value) {
+    // e = A^-1 g stays below about max|g| * n^2 / 2 on level 1 (n = its
+    // larger side); keep it below 2^14 in FP16
+    double n = (double)std::max(L1.w, L1.h);
+    kexp = std::max(0, (int)std::ceil(std::log2(0.5 * n * n)) - 14);
+  }
+  auto top_args = [&](int cin) {
+    MgArgsT<float, SC> a{};
+    a.in = L0.e[cin];
+    a.out = L0.e[1 - cin];
+    a.rhs = L0.rhs;
+    a.code = L0.code;
+    a.w = L0.w;
+    a.h = L0.h;
+    a.pitch = L0.pitch;
+    a.hh = L0.hh;
+    a.ihsq = 1.0f / L0.hh / L0.hh;
+    a.nsweeps = 3;
+    a.rfac = 1.0f / 16.0f;
+    for (int k = 0; k < 5; k++) {
+      a.wsum[k] = (float)((double)(float)k + 0.0001);
+      a.rwsum[k] = 1.0f / a.wsum[k];
+    }
+    a.alpha = 1.0f;
+    a.tile = -1;
+    a.ext = 1;
+    a.zgbc = 1;
+    a.cw = L1.w;
+    a.ch = L1.h;
+    a.cpitch = L1.pitch;
+    if (scaled) {
+      a.scale_bits = scale_bits;
+      a.scale_h1sq = L1.hh * L1.hh;
+      a.scale_kexp = kexp;
+    }
+    return a;
+  };
+  auto launch_top = [&](const MgArgsT<float, SC> &a) {
+    ProfScope ps_(KC_SMOOTH_L0, st);
+    if constexpr (scaled)
+      launch_mg_mixed_top<SC>(a, st);
+    else
+      launch_mg(a, st);
+  };
+  // down
+  {
+    MgArgsT<float, SC> a = top_args(0);
+    a.zero_init = 1;
+    a.rc = rhs(1);
+    launch_top(a);
+    cur[0] = 1;
+  }
+  for (int l = 1; l < T; l++) {
+    ProfScope ps_(l == 1 ? KC_SMOOTH_L1 : KC_SMOOTH_COARSE, st);
+    MgArgsT<SC> a = ext_level_args<SC>(mg, lo, l, cur[l], 3);
+    a.zero_init = 1;
+    a.rc = rhs(l + 1);
+    a.cw = mg.lv[l + 1].w;
+    a.ch = mg.lv[l + 1].h;
+    a.cpitch = mg.lv[l + 1].pitch;
+    launch_mg(a, st);
+    cur[l] ^= 1;
+  }
+  {
+    std::vector<float> rf(mg.levels, 0.25f);
+    run_tail_t<SC, float>(mg, T, rhs(T), arr(T, 0), scaled ? rf.data() : nullptr, st);
+    cur[T] = 0;
+  }
+  // up
+  for (int l = T - 1; l >= 1; l--) {
+    ProfScope ps_(l == 1 ? KC_SMOOTH_L1 : KC_SMOOTH_COARSE, st);
+    MgArgsT<SC> a = ext_level_args<SC>(mg, lo, l, cur[l], 3);
+    a.ec = arr(l + 1, cur[l + 1]);
+    a.codec = mg.lv[l + 1].code;
+    a.cpitch = mg.lv[l + 1].pitch;
+    a.cw = mg.lv[l + 1].w;
+    a.ch = mg.lv[l + 1].h;
+    launch_mg(a, st);
+    cur[l] ^= 1;
+  }
+  {
+    MgArgsT<float, SC> a = top_args(cur[0]);
+    a.ec = arr(1, cur[1]);
+    a.codec = L1.code;
+    launch_top(a);
+    cur[0] ^= 1;
+  }
+  mg.cur0 = cur[0];
+}
+}  // namespace
+
+size_t ext_hier_bytes(int W, int H) {
+  size_t total = 512;
+  for (auto &L : ext_shapes(W, H, 1.0f)) {
+    size_t n = (size_t)L.pitch * L.h;
+    total += 3 * align256(n * 4) + 2 * align256(n);
+  }
+  return total;
+}
+
+void ext_hier_alloc(MgHier &mg, int W, int H, float h0) {
+  mg_free(mg);
+  std::vector<MgLevel> lv = ext_shapes(W, H, h0);
+  init_kernel_attributes();
+  size_t total = ext_hier_bytes(W, H);
+  void *arena = nullptr;
+  if (cudaMalloc(&arena, total) != cudaSuccess) {
+    cudaGetLastError();
+    throw std::bad_alloc();
+  }
+  UBG_CUDA(cudaMemsetAsync(arena, 0, total, cudaStreamLegacy));
+  UBG_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
+  char *p = (char *)arena;
+  for (auto &L : lv) {
+    size_t n = (size_t)L.pitch * L.h;
+    L.e[0] = (float *)p;
+    p += align256(n * 4);
+    L.e[1] = (float *)p;
+    p += align256(n * 4);
+    L.rhs = (float *)p;
+    p += align256(n * 4);
+    L.flag = (uint8_t *)p;
+    p += align256(n);
+    L.code = (uint8_t *)p;
+    p += align256(n);
+  }
+  mg.norm = (double *)p;
+  mg.post_norm2 = nullptr;
+  mg.ext = true;
+  mg.ncoarse = 40;
+  mg.lv = lv;
+  mg.levels = (int)lv.size();
+  mg.tail_top = choose_tail(lv, 4096, 4, mg.levels - 1);
+  if (mg.tail_top < 1) mg.tail_top = mg.levels - 1;
+  mg.tail_top_fp64 = -1;
+  mg.arena = arena;
+  mg.arena_bytes = total;
+  mg.cur0 = 0;
+}
+
+void ext_hier_update_fields(MgHier &mg, const uint8_t *flag0, int pitch0, cudaStream_t st) {
+  ProfScope ps_(KC_COARSEN, st);
+  MgLevel &L0 = mg.lv[0];
+  UBG_CUDA(cudaMemcpy2DAsync(L0.flag, L0.pitch, flag0, pitch0, L0.w, L0.h,
+                             cudaMemcpyDeviceToDevice, st));
+  for (int l = 1; l < mg.levels; l++) {
+    MgLevel &F = mg.lv[l - 1], &C = mg.lv[l];
+    dim3 grid((C.w + 31) / 32, (C.h + 7) / 8);
+    k_coarsen_ext<<<grid, dim3(32, 8), 0, st>>>(F.flag, F.pitch, C.flag, C.w, C.h, C.pitch);
+    UBG_LAUNCH_CHECK();
+  }
+  for (int l = 0; l < mg.levels; l++) level_make_code(mg.lv[l], st);
+}
+
+void ext_vcycle(MgHier &mg, MgLow *lo, int prec, const unsigned *scale_bits, cudaStream_t st) {
+  if (prec == UBG_FP32)
+    ext_vcycle_t<float>(mg, nullptr, nullptr, st);
+  else if (prec == UBG_MIXED_FP16)
+    ext_vcycle_t<__half>(mg, lo, scale_bits, st);
+  else if (prec == UBG_MIXED_BF16)
+    ext_vcycle_t<__nv_bfloat16>(mg, lo, scale_bits, st);
+  else
+    throw ArgError("precision");
 }
 
 }  // namespace ubg

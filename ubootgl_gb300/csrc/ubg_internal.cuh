@@ -326,7 +326,14 @@ struct MgHier {
   size_t arena_bytes = 0;
   double *norm = nullptr;        // device scalar for residual norms
   double *post_norm2 = nullptr;  // if set: ||r||^2 after each level-0 post-smoothing
+  // The tolerance solver's own hierarchy (ext_hier_*): level sizes
+  // floor(w/2)+1, zero-gradient edges on every level, coarsest level = the
+  // last one, solved with `ncoarse` sweeps.  The reference's hierarchy
+  // (ext = false) ends one level earlier (levels-2) with 5 sweeps.
+  bool ext = false;
+  int ncoarse = 5;
 };
+inline int mg_coarsest(const MgHier &mg) { return mg.ext ? mg.levels - 1 : mg.levels - 2; }
 
 // Times the candidate smoother tiles of every level and the tail sizes on
 // this hierarchy's own arrays (state preserved: trials write only scratch
@@ -407,6 +414,60 @@ void mg_low_free(MgLow &lo);
 // the final p when tol > 0, else -1.
 int mg_solve_mixed(MgHier &mg, MgLow &lo, double tol, int max_cycles, double fnorm2, double *rel,
                    cudaStream_t st);
+
+// ------------------------------------------------ tolerance-mode solver
+// The tolerance solver's hierarchy (sizes floor(w/2)+1, zero-gradient
+// edges on every level; k_mg.cu) and one preconditioning V-cycle of it:
+// z = M r with r = level 0's rhs and z = level 0's e[cur0] after the call
+// (zero start).  prec selects the storage of the coarse levels: FP32 (mg's
+// arrays) or 16 bits (lo's arrays, h^2-scaled, scale from *scale_bits =
+// max|r| as float bits); level 0 is FP32 in every mode.
+size_t ext_hier_bytes(int W, int H);
+void ext_hier_alloc(MgHier &mg, int W, int H, float h0);
+// Level-0 flag from flag0 (pitch0 bytes per row), coarse flags, codes.
+void ext_hier_update_fields(MgHier &mg, const uint8_t *flag0, int pitch0, cudaStream_t st);
+void ext_vcycle(MgHier &mg, MgLow *lo, int prec, const unsigned *scale_bits, cudaStream_t st);
+
+// Device scalars of the flexible CG loop (k_krylov.cu).
+struct FcgScalars {
+  double ff;       // ||f_c||^2
+  double rr;       // ||r||^2 of the recurrence
+  double zq;       // (z, q_prev)
+  double dr;       // (d, r)
+  double dq[2];    // (d, q) of this and of the previous iteration
+  double fsum;     // sum of f over the interior fluid cells
+  double neast;    // fluid cells of the outflow column x = W-2
+  double nfluid;   // interior fluid cells
+  unsigned maxbits;  // max|r| as float bits
+  unsigned pad;
+};
+
+struct FcgSolver {
+  MgHier mg;  // the tolerance hierarchy (level 0: rhs = r, e = z)
+  MgLow lo;   // its 16-bit arrays (mixed precision)
+  int prec = UBG_FP32;
+  double *x = nullptr;  // FP64 pressure iterate, W x H pitched like the fields
+  float *d[2] = {nullptr, nullptr}, *q = nullptr;
+  FcgScalars *dev = nullptr, *host = nullptr;
+  void *arena = nullptr;
+  bool dirty = true;  // the flag changed since the coarse flags were built
+  int W = 0, H = 0, P = 0;
+  float h = 0.0f;
+};
+void fcg_alloc(FcgSolver &fs, int W, int H, int P, float h);
+void fcg_free(FcgSolver &fs);
+size_t fcg_bytes(int W, int H, int P, int prec);
+void fcg_set_precision(FcgSolver &fs, int prec);
+// Solves the zero-gradient system for p (warm start: p as given; result:
+// p's interior cells, and fs.x in FP64) until ||r|| <= tol ||f_c||, at most
+// max_iter iterations (one V-cycle each).  Synchronises once per
+// iteration.  Returns the iterations run; *rel = ||f_c + L x|| / ||f_c||
+// of the final x.
+int fcg_solve(FcgSolver &fs, const uint8_t *flag, const float *f, float *p, double tol,
+              int max_iter, double *rel, cudaStream_t st);
+// The pressure-gradient update from the FP64 pressure x.
+void launch_gradient64(const VelBufs &v, int fx, int fy, const double *x, const StepScalars *sc,
+                       unsigned *umax_bits, cudaStream_t st);
 
 // ------------------------------------------------------------- tracers
 struct TracerArgs {
