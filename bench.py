@@ -111,10 +111,17 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def time_cpu_step(W, H, budget_s=20.0, min_steps=3, max_steps=None, threads=None):
+def workload_name(W, H):
+    """config.workload of both arms."""
+    return "fluid step %dx%d, 12 discs, FP32, 2 V-cycles, dt=0.5h/max|u|" % (W, H)
+
+
+def time_cpu_step(W, H, budget_s=20.0, min_steps=3, max_steps=None, threads=None, warmup=1):
     """The reference step on the host cores: oracle/_ref (the reference's own
-    simulation.cpp built from source) where it builds (x86-64), else the C
-    restatement of it.  Returns (Mcell-steps/s, info)."""
+    simulation.cpp built from source with its own -Ofast -march=native) where
+    it builds (x86-64), else the C restatement of it built for speed (-O3
+    -ffast-math; the parity build of the restatement is never timed).
+    Returns (Mcell-steps/s, info)."""
     from oracle import oracle as O
     flag, vx, vy = workload(W, H)
     threads = threads or cpu_threads()
@@ -128,14 +135,14 @@ def time_cpu_step(W, H, budget_s=20.0, min_steps=3, max_steps=None, threads=None
     except Exception:
         sim = None
     if sim is None:
-        O.set_threads(threads)
-        sim = O.PortSim(flag)
+        O.set_threads(threads, fast=True)
+        sim = O.PortSim(flag, fast=True)
     for n in ("vx", "vy", "vx_back", "vy_back"):
         sim.set(n, vx if n.startswith("vx") else vy)
     from ubootgl_gb300 import workload as WL
     h = sim.h
-    # warm-up step
-    sim.step(WL.cfl_dt(sim.get("vx"), sim.get("vy"), h))
+    for _ in range(max(1, warmup)):
+        sim.step(WL.cfl_dt(sim.get("vx"), sim.get("vy"), h))
     n, t_total = 0, 0.0
     while True:
         dt = WL.cfl_dt(sim.get("vx"), sim.get("vy"), h)
@@ -147,8 +154,11 @@ def time_cpu_step(W, H, budget_s=20.0, min_steps=3, max_steps=None, threads=None
             break
     val = W * H * n / t_total / 1e6
     return val, {"kind": kind, "cores": threads, "steps": n, "seconds": t_total,
-                 "sample": "%dx%d full steps (2 V-cycles), %d timed after 1 warm-up; "
-                           "dt = 0.5 h/max|u| computed outside the timed call" % (W, H, n)}
+                 "build": ("reference sources, -Ofast -march=native" if kind == "reference"
+                           else "C restatement, -O3 -ffast-math -funroll-loops, OpenMP"),
+                 "sample": "%dx%d full steps (2 V-cycles), %d timed after %d warm-up; "
+                           "dt = 0.5 h/max|u| computed outside the timed call"
+                           % (W, H, n, max(1, warmup))}
 
 
 def run_reference(args):
@@ -157,19 +167,20 @@ def run_reference(args):
         return
     W, H = args.width, args.height
     steps = max(1, args.steps)
-    # each timed step is one full CPU step of the workload; the number of
-    # timed steps is bounded so that the run ends within a few minutes
-    val, info = time_cpu_step(W, H, budget_s=30.0, min_steps=1, max_steps=min(steps, 200))
+    # each timed step is one full CPU step of the workload: K steps after W
+    # warm-up steps, as the GPU arm (at ~0.1 s per step on 16 cores the
+    # default run takes a few seconds; K is capped at 500)
+    val, info = time_cpu_step(W, H, budget_s=0.0, min_steps=min(steps, 500),
+                              max_steps=min(steps, 500), warmup=args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "Mcell-steps/s",
-        "n_gpus": args.gpus, "steps": info["steps"], "warmup": 1,
+        "n_gpus": args.gpus, "steps": info["steps"], "warmup": args.warmup,
         "ms_per_step": round(1e3 * info["seconds"] / info["steps"], 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded disc mask + smoothed-noise velocity)",
-        "config": {"workload": "fluid step %dx%d, 12 discs, 2 V-cycles" % (W, H),
-                   "parallelism": "host cores"},
+        "config": {"workload": workload_name(W, H), "parallelism": "host cores"},
         "cpu_baseline": {"value": round(val, 3), "unit": "Mcell-steps/s", "cores": info["cores"],
-                         "kind": info["kind"], "sample": info["sample"]},
+                         "kind": info["kind"], "sample": info["sample"], "build": info["build"]},
         "e2e": {"value": round(val, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -286,8 +297,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded disc mask + smoothed-noise velocity)",
-        "config": {"workload": "fluid step %dx%d, 12 discs, FP32, 2 V-cycles, dt=0.5h/max|u| on device"
-                               % (W, H),
+        "config": {"workload": workload_name(W, H),
                    "solver": "FP32 drop-in: the reference's step with its 2 V-cycles (value); "
                              "tolerance solver (FP32 / FP16 / BF16 coarse levels, residual "
                              "<= tol) and fixed mixed solvers in modes; served stream in served",
@@ -311,7 +321,7 @@ def run_ours(args):
         val, info = time_cpu_step(W, H, budget_s=args.cpu_budget)
         line["cpu_baseline"] = {"value": round(val, 3), "unit": "Mcell-steps/s",
                                 "cores": info["cores"], "kind": info["kind"],
-                                "sample": info["sample"]}
+                                "sample": info["sample"], "build": info["build"]}
     print(json.dumps(line), flush=True)
 
 

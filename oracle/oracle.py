@@ -18,6 +18,7 @@ FIELD = {"vx": 0, "vy": 1, "vx_back": 2, "vy_back": 3, "p": 4, "f": 5, "flag": 6
          "vx_accum": 7, "vy_accum": 8}
 
 _port = None
+_port_fast = None
 _ref = None
 
 
@@ -25,50 +26,59 @@ def _fp(a, ct):
     return a.ctypes.data_as(C.POINTER(ct))
 
 
-def port_lib():
-    global _port
+def port_lib(fast=False):
+    """The restatement built for parity (default) or, with fast, the same
+    sources built for speed (the CPU baseline timing only)."""
+    global _port, _port_fast
+    if fast:
+        if _port_fast is None:
+            _port_fast = _bind_port(C.CDLL(build_oracle.build(fast=True)))
+        return _port_fast
     if _port is None:
-        lib = C.CDLL(build_oracle.build())
-        for sfx, ct in (("f", C.c_float), ("d", C.c_double)):
-            P = C.POINTER(ct)
-            g = lambda n: getattr(lib, "ubo_%s_%s" % (sfx, n))
-            g("create").restype = C.c_void_p
-            g("create").argtypes = [P, C.c_int, C.c_int, ct, ct]
-            g("destroy").argtypes = [C.c_void_p]
-            for n in ("step",):
-                g(n).argtypes = [C.c_void_p, ct]
-            g("step_ncycles").argtypes = [C.c_void_p, ct, C.c_int]
-            g("set_dt").argtypes = [C.c_void_p, ct]
-            for n in ("apply_accum", "diffuse", "advect", "set_vbcs", "set_pbc", "project"):
-                g(n).argtypes = [C.c_void_p]
-            g("project_ncycles").argtypes = [C.c_void_p, C.c_int]
-            g("project_opts").argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
-            g("sim_mg_solve").argtypes = [C.c_void_p, C.c_int]
-            g("get_field").argtypes = [C.c_void_p, C.c_int, P]
-            g("set_field").argtypes = [C.c_void_p, C.c_int, P]
-            g("update_flag").argtypes = [C.c_void_p, P]
-            g("get_h").restype = ct
-            g("get_h").argtypes = [C.c_void_p]
-            g("mg_levels").argtypes = [C.c_void_p]
-            g("mg_level_flag").argtypes = [C.c_void_p, C.c_int, P]
-            g("mg_level_size").argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int),
-                                           C.POINTER(C.c_int)]
-            g("add_sink").argtypes = [C.c_void_p, ct, ct, ct]
-            g("mg_create").restype = C.c_void_p
-            g("mg_create").argtypes = [C.c_int, C.c_int, P]
-            g("mg_destroy").argtypes = [C.c_void_p]
-            g("mg_nlevels").argtypes = [C.c_void_p]
-            g("mg_solve").argtypes = [C.c_void_p, P, P, P, ct, C.c_int]
-            g("rbgs").argtypes = [P, P, P, C.c_int, C.c_int, ct, ct]
-            g("residual").restype = C.c_double
-            g("residual").argtypes = [P, P, P, P, C.c_int, C.c_int, ct]
-            g("advect_mask_vx").argtypes = [P, C.c_int, C.c_int, C.c_int]
-            g("advect_mask_vy").argtypes = [P, C.c_int, C.c_int, C.c_int]
-        lib.ubo_omp_set_threads.argtypes = [C.c_int]
-        if hasattr(lib, "ubo_tracers_f_step"):
-            _bind_tracers(lib)
-        _port = lib
+        _port = _bind_port(C.CDLL(build_oracle.build()))
     return _port
+
+
+def _bind_port(lib):
+    for sfx, ct in (("f", C.c_float), ("d", C.c_double)):
+        P = C.POINTER(ct)
+        g = lambda n: getattr(lib, "ubo_%s_%s" % (sfx, n))
+        g("create").restype = C.c_void_p
+        g("create").argtypes = [P, C.c_int, C.c_int, ct, ct]
+        g("destroy").argtypes = [C.c_void_p]
+        for n in ("step",):
+            g(n).argtypes = [C.c_void_p, ct]
+        g("step_ncycles").argtypes = [C.c_void_p, ct, C.c_int]
+        g("set_dt").argtypes = [C.c_void_p, ct]
+        for n in ("apply_accum", "diffuse", "advect", "set_vbcs", "set_pbc", "project"):
+            g(n).argtypes = [C.c_void_p]
+        g("project_ncycles").argtypes = [C.c_void_p, C.c_int]
+        g("project_opts").argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+        g("sim_mg_solve").argtypes = [C.c_void_p, C.c_int]
+        g("get_field").argtypes = [C.c_void_p, C.c_int, P]
+        g("set_field").argtypes = [C.c_void_p, C.c_int, P]
+        g("update_flag").argtypes = [C.c_void_p, P]
+        g("get_h").restype = ct
+        g("get_h").argtypes = [C.c_void_p]
+        g("mg_levels").argtypes = [C.c_void_p]
+        g("mg_level_flag").argtypes = [C.c_void_p, C.c_int, P]
+        g("mg_level_size").argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int)]
+        g("add_sink").argtypes = [C.c_void_p, ct, ct, ct]
+        g("mg_create").restype = C.c_void_p
+        g("mg_create").argtypes = [C.c_int, C.c_int, P]
+        g("mg_destroy").argtypes = [C.c_void_p]
+        g("mg_nlevels").argtypes = [C.c_void_p]
+        g("mg_solve").argtypes = [C.c_void_p, P, P, P, ct, C.c_int]
+        g("rbgs").argtypes = [P, P, P, C.c_int, C.c_int, ct, ct]
+        g("residual").restype = C.c_double
+        g("residual").argtypes = [P, P, P, P, C.c_int, C.c_int, ct]
+        g("advect_mask_vx").argtypes = [P, C.c_int, C.c_int, C.c_int]
+        g("advect_mask_vy").argtypes = [P, C.c_int, C.c_int, C.c_int]
+    lib.ubo_omp_set_threads.argtypes = [C.c_int]
+    if hasattr(lib, "ubo_tracers_f_step"):
+        _bind_tracers(lib)
+    return lib
 
 
 def _bind_tracers(lib):
@@ -157,8 +167,8 @@ def field_shape(name, W, H):
 class PortSim:
     """The CPU restatement's Simulation (dtype float32 or float64)."""
 
-    def __init__(self, flag, pwidth=1.0, mu=1e-4, dtype=np.float32):
-        self.lib = port_lib()
+    def __init__(self, flag, pwidth=1.0, mu=1e-4, dtype=np.float32, fast=False):
+        self.lib = port_lib(fast)
         self.dtype = np.dtype(dtype)
         self.sfx = "f" if self.dtype == np.float32 else "d"
         self.ct = C.c_float if self.sfx == "f" else C.c_double
@@ -337,8 +347,8 @@ def port_residual(p, f, flag, h, dtype=np.float32):
     return r, n
 
 
-def set_threads(n):
-    port_lib().ubo_omp_set_threads(n)
+def set_threads(n, fast=False):
+    port_lib(fast).ubo_omp_set_threads(n)
 
 
 # ---------------------------------------------------------------------------

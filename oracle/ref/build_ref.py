@@ -19,7 +19,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT_DIR = os.path.join(ORACLE, "_ref")
 OUT = os.path.join(OUT_DIR, "libubgref.so")
-REF_ROOT = os.environ.get("UBG_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: UBG_REFERENCE_ROOT, else a directory "reference"
+# beside the repository
+REF_ROOT = os.environ.get("UBG_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(ORACLE)), "reference"))
 
 
 def available() -> bool:

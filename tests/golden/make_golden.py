@@ -12,9 +12,16 @@ inputs and stores inputs and outputs as compressed .npz files:
   levels_257x129.npz the multigrid flag hierarchy (MG::updateFields)
   mg_laplace_65.npz  mgtest.cpp's Laplace problem (sinh(pi y) sin(pi x)
                      Dirichlet data, all flags 1, MG(N, N)) after 5 V-cycles
+  long_1024x512.npz  the 1024x512, 12-disc flow of the benchmark's first
+                     configuration over 100 steps: the dt of every step and,
+                     after steps 0, 24, 49, 74 and 99, sampled rows and
+                     columns of vx, vy and p plus their sum, L2 norm and
+                     max|.| (the full fields would be 6 MB per kept step).
+                     The inputs are regenerated from their seeds by the
+                     test; a SHA-256 of them is stored to prove it.
 
 Run from the repository root on an x86-64 machine with the reference
-checkout:  python tests/golden/make_golden.py
+checkout:  python tests/golden/make_golden.py [steps|stages|levels|mgtest|long ...]
 """
 import os
 import sys
@@ -50,6 +57,54 @@ def run_steps(W, H, nsteps, seed):
                         dt=np.array(dts, np.float32), kept=np.array(kept),
                         vx=np.stack([vxs[k] for k in kept]), vy=np.stack([vys[k] for k in kept]),
                         p=np.stack([ps[k] for k in kept]), h=np.float32(ref.h))
+
+
+LONG = dict(W=1024, H=512, steps=100, seed=2024, kept=(0, 24, 49, 74, 99),
+            rows=(100, 256, 400), cols=(300, 700))
+
+
+def long_inputs():
+    W, H, seed = LONG["W"], LONG["H"], LONG["seed"]
+    flag = WL.disc_flag(W, H, n_discs=12, r_range=(20, 60), seed=seed)
+    vx0, vy0 = WL.initial_velocity(flag, seed=seed + 1)
+    return flag, vx0, vy0
+
+
+def inputs_digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, np.float32).tobytes())
+    return h.hexdigest()
+
+
+def samples(a):
+    a64 = a.astype(np.float64)
+    rows = np.stack([a[r] for r in LONG["rows"]])
+    cols = np.stack([a[:, c] for c in LONG["cols"]])
+    stats = np.array([a64.sum(), np.sqrt((a64 * a64).sum()), np.abs(a64).max()])
+    return rows, cols, stats
+
+
+def run_long():
+    flag, vx0, vy0 = long_inputs()
+    ref = O.RefSim(flag, 1.0, 1e-4)
+    for n, a in (("vx", vx0), ("vy", vy0), ("vx_back", vx0), ("vy_back", vy0)):
+        ref.set(n, a)
+    out = {"digest": np.array(inputs_digest(flag, vx0, vy0)), "kept": np.array(LONG["kept"])}
+    dts = []
+    for k in range(LONG["steps"]):
+        dt = WL.cfl_dt(ref.get("vx"), ref.get("vy"), ref.h)
+        ref.step(dt)
+        dts.append(dt)
+        if k in LONG["kept"]:
+            for n in ("vx", "vy", "p"):
+                rows, cols, stats = samples(ref.get(n))
+                out["%s_rows_%d" % (n, k)] = rows
+                out["%s_cols_%d" % (n, k)] = cols
+                out["%s_stats_%d" % (n, k)] = stats
+    out["dt"] = np.array(dts, np.float32)
+    np.savez_compressed(os.path.join(HERE, "long_1024x512.npz"), **out)
 
 
 def run_stages():
@@ -105,11 +160,18 @@ def run_mgtest():
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("the reference checkout (x86-64) is needed to generate fixtures")
-    for case in STEP_CASES:
-        run_steps(*case)
-    run_stages()
-    run_levels()
-    run_mgtest()
+    only = sys.argv[1:]
+    if not only or "steps" in only:
+        for case in STEP_CASES:
+            run_steps(*case)
+    if not only or "stages" in only:
+        run_stages()
+    if not only or "levels" in only:
+        run_levels()
+    if not only or "mgtest" in only:
+        run_mgtest()
+    if not only or "long" in only:
+        run_long()
     for fn in sorted(os.listdir(HERE)):
         if fn.endswith(".npz"):
             print(fn, os.path.getsize(os.path.join(HERE, fn)))

@@ -83,3 +83,49 @@ def test_mgtest_laplace_matches_reference():
     exact = np.sinh(np.pi * yy) * np.sin(np.pi * xx)
     err0 = np.abs(exact[1:-1, 1:-1]).max()
     assert np.abs(u[1:-1, 1:-1] - exact[1:-1, 1:-1]).max() < 0.5 * err0
+
+
+# The benchmark's first configuration over its full length: 1024x512, 12
+# discs, 100 steps of the reference (long_1024x512.npz, classic red-black
+# schedule), against the restatement with the same dt sequence.  Measured
+# max |difference| / max |field| over the sampled rows and columns, per kept
+# step (the restatement's plain IEEE order against the reference's -Ofast):
+#   step            0       24      49      74      99
+#   vx, vy        6.2e-6  1.9e-6  5.8e-6  8.7e-6  9.2e-6
+#   p             4.3e-6  1.8e-5  2.1e-4  1.3e-4  6.9e-5
+# p moves most: two V-cycles leave it unconverged, so rounding differences
+# persist through the warm start.  The bounds below are ~2.5x those, and the
+# GPU path equals the restatement bit for bit over the same 100 steps
+# (test_gpu_parity.py), which chains the GPU to the reference at full length.
+LONG_VEL_TOL = {0: 1.5e-5, 24: 1.5e-5, 49: 2e-5, 74: 2.5e-5, 99: 2.5e-5}
+LONG_P_TOL = {0: 1.5e-5, 24: 5e-5, 49: 5e-4, 74: 4e-4, 99: 2e-4}
+
+
+def test_100_steps_1024x512_match_reference():
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_golden as MG
+    z = np.load(os.path.join(GOLD, "long_1024x512.npz"))
+    flag, vx0, vy0 = MG.long_inputs()
+    if MG.inputs_digest(flag, vx0, vy0) != str(z["digest"]):
+        pytest.skip("the seeded inputs differ on this platform from the ones the fixture was made with")
+    sim = O.PortSim(flag)
+    for n, a in (("vx", vx0), ("vy", vy0), ("vx_back", vx0), ("vy_back", vy0)):
+        sim.set(n, a)
+    kept = [int(k) for k in z["kept"]]
+    N = flag.size
+    for k, dt in enumerate(z["dt"]):
+        sim.step(np.float32(dt))
+        if k not in kept:
+            continue
+        for n in ("vx", "vy", "p"):
+            rows, cols, stats = MG.samples(sim.get(n))
+            zr, zc, zs = z["%s_rows_%d" % (n, k)], z["%s_cols_%d" % (n, k)], z["%s_stats_%d" % (n, k)]
+            tol = LONG_P_TOL[k] if n == "p" else LONG_VEL_TOL[k]
+            err = max(np.abs(rows.astype(np.float64) - zr).max(),
+                      np.abs(cols.astype(np.float64) - zc).max()) / zs[2]
+            assert err < tol, (n, k, err)
+            # L2 norm and max|.| relative; the sum relative to sqrt(N) * L2
+            assert abs(stats[1] - zs[1]) < tol * zs[1], (n, k)
+            assert abs(stats[2] - zs[2]) < tol * zs[2], (n, k)
+            assert abs(stats[0] - zs[0]) < tol * np.sqrt(N) * zs[1], (n, k)
