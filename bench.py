@@ -259,6 +259,9 @@ def run_ours(args):
     if rank != 0:
         return
 
+    # ---- the plain FP32 step at scale with tracers (8192 x 4096)
+    scale = scale_bench(L, lib, args.scale_steps, args.warmup, dev) if args.scale_steps > 0 else {}
+
     # ---- the solver modes on the same workload (extensions): the tolerance
     # solver in FP32 / FP16 / BF16 to the same relative residual, and the
     # fixed two-cycle mixed solvers
@@ -314,6 +317,7 @@ def run_ours(args):
         "kernels": kt["detail"],
         "profiled_step_ms": kt["profiled_step_ms"],
         "modes": modes,
+        "scale": scale,
         "batched": batched,
         "served": served,
     }
@@ -596,6 +600,103 @@ def profiled_traffic(W, H):
     return None
 
 
+def scale_bench(L, lib, steps, warmup, dev, W=8192, H=4096, ntr=1 << 20, npts=30):
+    """The plain FP32 step at scale: one 8192 x 4096 grid (33.5 M cells),
+    400 seeded discs of radius 20-60 cells, 2^20 tracers (ring of 30 points,
+    draw_tracers_cs.cpp:97) advected every step; `steps` steps of fluid step
+    + tracer step, CUDA events on the simulation's stream.  Reports per
+    kernel class its mean launch time and algorithmic GB/s, the tracer step
+    alone, and the V-cycles per projection (the reference's 2; the tolerance
+    solver's count to 1e-6 at this size for comparison)."""
+    import ctypes as C
+    import torch
+    from ubootgl_gb300 import workload as WL
+    from ubootgl_gb300.simulation import Simulation, Tracers
+    flag = WL.disc_flag(W, H, n_discs=400, r_range=(20.0 * 1024 / W, 60.0 * 1024 / W), seed=2026)
+    vx, vy = WL.initial_velocity(flag, seed=2027)
+    sim = Simulation(flag, 1.0, 1e-4)
+    for n, a in (("vx", vx), ("vy", vy), ("vx_back", vx), ("vy_back", vy)):
+        sim.set(n, a)
+    pdim = (np.float32(1.0), np.float32(np.float32(1.0) * np.float32(H) / np.float32(W)))
+    tr = Tracers(sim, ntr, npts)
+    tr.upload(*WL.seed_tracers(flag, ntr, npts, pdim, seed=2028))
+    stream = C.c_void_p()
+    L.check(lib.ubg_stream(sim._h, C.byref(stream)))
+    ext = torch.cuda.ExternalStream(stream.value, device=dev)
+    sim.autotune()
+    k = 0
+    for _ in range(max(3, warmup)):
+        sim.step_cfl(0.5)
+        tr.step(sim.last_dt(), 7 + k)
+        k += 1
+    sim.sync()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record(ext)
+    for _ in range(steps):
+        sim.step_cfl(0.5)
+        tr.step(sim.last_dt(), 7 + k)
+        k += 1
+    e1.record(ext)
+    sim.sync()
+    ms = e0.elapsed_time(e1)
+    # the tracer step alone
+    reps = 20
+    dt = sim.last_dt()
+    e0.record(ext)
+    for i in range(reps):
+        tr.step(dt, 100 + i)
+    e2.record(ext)
+    sim.sync()
+    tr_ms = e0.elapsed_time(e2) / reps
+    # per kernel class (direct launches with event pairs)
+    sim.profile(True)
+    sim.profile_reset()
+    nprof = 5
+    for _ in range(nprof):
+        sim.step_cfl(0.5)
+    sim.sync()
+    classes = sim.profile_classes()
+    sim.profile(False)
+    peak = measured_peaks().get("hbm_gbs") or 6800.0
+    cells = W * H
+    kern = {}
+    for name, (kms, n) in sorted(classes.items(), key=lambda kv: -kv[1][0]):
+        d = {"ms_per_step": round(kms / nprof, 4), "launches_per_step": round(n / nprof, 1),
+             "mean_launch_ms": round(kms / n, 5)}
+        if name in ALG_BYTES_PER_CELL:
+            gbs = ALG_BYTES_PER_CELL[name] * cells / (kms / n / 1e3) / 1e9
+            d["alg_gbs"] = round(gbs, 1)
+            d["frac_of_measured_hbm"] = round(gbs / peak, 3)
+        kern[name] = d
+    vcycles = sim.solver_stats()[0]
+    tr_alg = 36.0 * ntr
+    finite = bool(np.isfinite(sim.get("p")).all())
+    pts, st, en, ag = tr.download()
+    heads = pts[np.arange(ntr), en % npts]
+    inside = float(np.mean((heads[:, 0] >= 0) & (heads[:, 0] <= pdim[0]) &
+                           (heads[:, 1] >= 0) & (heads[:, 1] <= pdim[1])))
+    del tr
+    # the tolerance solver's V-cycles to 1e-6 at this size (3 steps)
+    sim.set_options(solver_mode=L.SOLVE_TOLERANCE, tol=1e-6, max_vcycles=200)
+    tol_cycles = []
+    for _ in range(3):
+        sim.step_cfl(0.5)
+        tol_cycles.append(sim.solver_stats())
+    sim.close()
+    return {"workload": "fluid step %dx%d, 400 discs r 20-60 cells (%.1f %% solid), FP32, "
+                        "2 V-cycles, dt=0.5h/max|u|, + %d tracers x %d points"
+                        % (W, H, 100.0 * (1.0 - flag.mean()), ntr, npts),
+            "steps": steps, "value": round(cells * steps / (ms / 1e3) / 1e6, 2),
+            "unit": "Mcell-steps/s (fluid + tracer step)", "ms_per_step": round(ms / steps, 4),
+            "tracer_step_ms": round(tr_ms, 4),
+            "tracer_alg_gbs": round(tr_alg / (tr_ms / 1e3) / 1e9, 1),
+            "tracer_alg_bytes": "36 B per tracer (positions r/w, ring pointers, age) plus the "
+                                "velocity / flag gathers",
+            "vcycles_per_projection": vcycles, "tolerance_vcycles_to_1e-6":
+                [[c, float("%.2e" % r)] for c, r in tol_cycles],
+            "kernels": kern, "fields_finite": finite, "tracer_heads_inside": round(inside, 4)}
+
+
 def kernel_timing(sim, lib, W, H, reps=30):
     """Per-kernel durations from CUDA events on the simulation's stream,
     recorded around every launch of `reps` further steps (direct launches:
@@ -709,6 +810,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--mode-steps", type=int, default=500,
                     help="timed steps per fixed-mode mixed-precision solver (0: skip)")
+    ap.add_argument("--scale-steps", type=int, default=50,
+                    help="steps of the 8192x4096 + 2^20 tracers leg (0: skip)")
     ap.add_argument("--tol-steps", type=int, default=10,
                     help="timed steps per tolerance-mode precision (0: skip)")
     ap.add_argument("--tol", type=float, default=1e-6,

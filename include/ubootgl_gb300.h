@@ -395,16 +395,17 @@ int ubg_mg_solve_device(ubg_mg *mg, float *p, int p_pitch, const float *f, int f
 
 /* Allocation-free solve.  No counterpart in the reference: it is the
  * ubg_mg_create(flag) + ubg_mg_solve_device pair for callers that must not
- * allocate GPU memory while they run (work recorded into a larger CUDA
- * graph, a fixed device-memory budget owned by a host framework, real-time
- * loops that must not reach the allocator).  The caller passes device
+ * allocate GPU memory while they run (a fixed device-memory budget owned by
+ * a host framework, real-time loops that must not reach the allocator,
+ * plug-ins whose host owns every device allocation).  The caller passes device
  * arrays p (in/out), f and flag (bytes 0 / 1), each with its row pitch in
  * elements; the solver's scratch (the level hierarchy) lives in one static
  * 24 MiB device array per GPU, held until the process exits.  Grids whose
  * hierarchy needs more (about 14 bytes x width rounded up to 32 x height x
  * 4/3; 1024 x 1024 fits, 2048 x 1024 does not) return UBG_EINVAL.  The first
  * call on a device looks up the array's address (cudaGetSymbolAddress): make
- * it before any stream capture.  Calls share the array: calls that overlap
+ * it before any stream capture (on a capturing stream it returns UBG_ESTATE).
+ * h must be finite and > 0.  Calls share the array: calls that overlap
  * on the GPU race.  Enqueued on `stream` (a cudaStream_t, NULL = the legacy
  * default stream); returns once enqueued. */
 int ubg_mg_solve_noalloc(float *p, int p_pitch, const float *f, int f_pitch, const uint8_t *flag,

@@ -912,7 +912,6 @@ struct ubg_tracers {
   float2 *points = nullptr;
   uint32_t *start = nullptr, *end = nullptr;
   float *ages = nullptr;
-  float2 *vxy = nullptr;
   ~ubg_tracers() {
     if (sim && sim->st) cudaStreamSynchronize(sim->st);
     if (mem) cudaFree(mem);
@@ -946,9 +945,8 @@ int ubg_tracers_create(ubg_sim *s, int ntracers, int npoints, ubg_tracers **out)
     t->ntr = ntracers;
     t->npts = npoints;
     size_t np = (size_t)ntracers * npoints * 8, nt = (size_t)ntracers * 4;
-    size_t ntex = (size_t)(2 * s->W - 1) * (2 * s->H - 1) * 8;
     auto al = [](size_t v) { return (v + 255) / 256 * 256; };
-    size_t total = al(np) + 3 * al(nt) + al(ntex);
+    size_t total = al(np) + 3 * al(nt);
     if (cudaMalloc(&t->mem, total) != cudaSuccess) {
       cudaGetLastError();
       throw std::bad_alloc();
@@ -958,8 +956,7 @@ int ubg_tracers_create(ubg_sim *s, int ntracers, int npoints, ubg_tracers **out)
     t->points = (float2 *)p; p += al(np);
     t->start = (uint32_t *)p; p += al(nt);
     t->end = (uint32_t *)p; p += al(nt);
-    t->ages = (float *)p; p += al(nt);
-    t->vxy = (float2 *)p;
+    t->ages = (float *)p;
     s->sync();
     *out = t.release();
     return UBG_OK;
@@ -1007,16 +1004,16 @@ int ubg_tracers_step(ubg_tracers *t, float dt, uint32_t rand_seed) {
   return guarded([&] {
     if (!t) throw ArgError("null handle");
     ubg_sim *s = t->sim;
-    launch_velocity_texture(s->v.vx[s->fx], s->v.vy[s->fy], s->P, s->W, s->H, t->vxy, nullptr,
-                            s->st);
     TracerArgs a{};
     a.points = t->points;
     a.start = t->start;
     a.end = t->end;
     a.ages = t->ages;
-    a.vxy = t->vxy;
-    a.tw = 2 * s->W - 1;
-    a.th = 2 * s->H - 1;
+    a.vx = s->v.vx[s->fx];
+    a.vy = s->v.vy[s->fy];
+    a.P = s->P;
+    a.W = s->W;
+    a.H = s->H;
     a.flag = s->flag();
     a.nfx = s->W;
     a.nfy = s->H;

@@ -195,17 +195,22 @@ __global__ void k_div_check(const float *x, int n, float d, float r, unsigned *b
 }  // namespace
 
 int selftest_div_rn(const float *x, int n, float d, unsigned *mismatches) {
-  float *dx = nullptr;
-  unsigned *dbad = nullptr;
-  UBG_CUDA(cudaMalloc(&dx, (size_t)n * sizeof(float)));
-  UBG_CUDA(cudaMalloc(&dbad, sizeof(unsigned)));
+  // both buffers are freed on every path, including a failing CUDA call
+  struct DevBuf {
+    void *p = nullptr;
+    ~DevBuf() {
+      if (p) cudaFree(p);
+    }
+  } bx, bb;
+  UBG_CUDA(cudaMalloc(&bx.p, (size_t)n * sizeof(float)));
+  UBG_CUDA(cudaMalloc(&bb.p, sizeof(unsigned)));
+  float *dx = (float *)bx.p;
+  unsigned *dbad = (unsigned *)bb.p;
   UBG_CUDA(cudaMemcpy(dx, x, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
   UBG_CUDA(cudaMemset(dbad, 0, sizeof(unsigned)));
   k_div_check<<<(n + 255) / 256, 256>>>(dx, n, d, 1.0f / d, dbad);
   UBG_LAUNCH_CHECK();
   UBG_CUDA(cudaMemcpy(mismatches, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost));
-  cudaFree(dx);
-  cudaFree(dbad);
   return 0;
 }
 }  // namespace ubg

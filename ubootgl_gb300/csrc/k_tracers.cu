@@ -14,6 +14,13 @@
 //                      in s, REPEAT in t) is < 0.6, reseed from
 //                      wang_hash(gid + seed) and the Numerical Recipes LCG
 //                      once the age exceeds 2*3.141, else advance the ring.
+//                      The reference samples the display texture, which the
+//                      GL path rebuilds every frame; here each lookup forms
+//                      the four texels it blends straight from the
+//                      staggered vx / vy with the texture kernel's own
+//                      arithmetic (texel()), so no (2W-1) x (2H-1) texture
+//                      is written per step (1.07 GB at 8192 x 4096) and the
+//                      results are the same bits.
 // One thread per texel / tracer; arithmetic in the shaders' order (FP32
 // weights instead of GL's fixed-point filter weights).
 #include "ubg_internal.cuh"
@@ -48,30 +55,40 @@ __device__ __forceinline__ float tex_f(const float *__restrict__ t, int P, int n
   return r0 * (1.0f - b) + r1 * b;
 }
 
+// Texel (i, j) of the display texture (interp_shader.cs:20-31).
+__device__ __forceinline__ float2 texel(const float *__restrict__ vx, const float *__restrict__ vy,
+                                        int P, int W, int H, int i, int j) {
+  float sx = (float)i / (2.0f * (float)W - 2.0f), tx = (float)(j + 1) / (2.0f * (float)H);
+  float sy = (float)(i + 1) / (2.0f * (float)W), ty = (float)j / (2.0f * (float)H - 2.0f);
+  return make_float2(tex_f(vx, P, W - 1, H, sx, tx), tex_f(vy, P, W, H - 1, sy, ty));
+}
+
 __global__ void k_velocity_texture(const float *__restrict__ vx, const float *__restrict__ vy,
                                    int P, int W, int H, float2 *vxy, float *mag) {
   int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
   int tw = 2 * W - 1, th = 2 * H - 1;
   if (i >= tw || j >= th) return;
-  float sx = (float)i / (2.0f * (float)W - 2.0f), tx = (float)(j + 1) / (2.0f * (float)H);
-  float sy = (float)(i + 1) / (2.0f * (float)W), ty = (float)j / (2.0f * (float)H - 2.0f);
-  float a = tex_f(vx, P, W - 1, H, sx, tx);
-  float b = tex_f(vy, P, W, H - 1, sy, ty);
+  const float2 t = texel(vx, vy, P, W, H, i, j);
+  const float a = t.x, b = t.y;
   size_t k = (size_t)j * tw + i;
   vxy[k] = make_float2(a, b);
   if (mag) mag[k] = sqrtf(a * a + b * b);
 }
 
-__device__ __forceinline__ float2 tex_vxy(const float2 *__restrict__ t, int nx, int ny, float s,
-                                          float tt) {
+// Bilinear lookup of the display texture (REPEAT in both directions), its
+// four texels formed from the staggered fields.
+__device__ __forceinline__ float2 tex_vxy(const float *__restrict__ vx,
+                                          const float *__restrict__ vy, int P, int W, int H,
+                                          float s, float tt) {
+  const int nx = 2 * W - 1, ny = 2 * H - 1;
   int i0, j0;
   float a = frac_floor(s * (float)nx - 0.5f, i0);
   float b = frac_floor(tt * (float)ny - 0.5f, j0);
   int i1 = wrap_repeat(i0 + 1, nx), j1 = wrap_repeat(j0 + 1, ny);
   i0 = wrap_repeat(i0, nx);
   j0 = wrap_repeat(j0, ny);
-  float2 t00 = t[(size_t)j0 * nx + i0], t10 = t[(size_t)j0 * nx + i1];
-  float2 t01 = t[(size_t)j1 * nx + i0], t11 = t[(size_t)j1 * nx + i1];
+  float2 t00 = texel(vx, vy, P, W, H, i0, j0), t10 = texel(vx, vy, P, W, H, i1, j0);
+  float2 t01 = texel(vx, vy, P, W, H, i0, j1), t11 = texel(vx, vy, P, W, H, i1, j1);
   float2 r;
   float r0 = t00.x * (1.0f - a) + t10.x * a;
   float r1 = t01.x * (1.0f - a) + t11.x * a;
@@ -116,9 +133,9 @@ __global__ void __launch_bounds__(256) k_tracers(TracerArgs a) {
   uint32_t curr = e % (uint32_t)a.npoints, next = (e + 1u) % (uint32_t)a.npoints;
   float2 cp = a.points[base + curr];
   const float pdx = a.pdx, pdy = a.pdy, dt = a.dt;
-  float2 v1 = tex_vxy(a.vxy, a.tw, a.th, cp.x / pdx, cp.y / pdy);
+  float2 v1 = tex_vxy(a.vx, a.vy, a.P, a.W, a.H, cp.x / pdx, cp.y / pdy);
   float mx = cp.x + v1.x * dt * 0.5f, my = cp.y + v1.y * dt * 0.5f;
-  float2 v2 = tex_vxy(a.vxy, a.tw, a.th, mx / pdx, my / pdy);
+  float2 v2 = tex_vxy(a.vx, a.vy, a.P, a.W, a.H, mx / pdx, my / pdy);
   float nx = cp.x + v2.x * dt, ny = cp.y + v2.y * dt;
   bool out = cp.x < 0.0f || cp.y < 0.0f || cp.x > pdx || cp.y > pdy;
   float fl = tex_flag(a.flag, a.fpitch, a.nfx, a.nfy, cp.x / pdx, cp.y / pdy);

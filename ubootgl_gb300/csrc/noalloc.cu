@@ -5,11 +5,12 @@
 // from cudaMalloc.
 //
 // It exists for callers that must not allocate GPU memory while they run:
-// code that records its work into a larger CUDA graph or runs under a
-// fixed device-memory budget handed out by a host framework, real-time
-// loops that must never reach the allocator, or plug-ins whose host
-// application owns every device allocation.  Such callers still pass their
-// own input and output arrays; only the solver's scratch comes from here.
+// code that runs under a fixed device-memory budget handed out by a host
+// framework, real-time loops that must never reach the allocator (a
+// cudaMalloc can synchronise the device and stall for milliseconds), or
+// plug-ins whose host application owns every device allocation.  Such
+// callers still pass their own input and output arrays; only the solver's
+// scratch comes from here.
 //
 // Limits and behaviour:
 //  - The scratch array is kNoAllocScratchBytes (24 MiB) on every GPU that
@@ -25,9 +26,12 @@
 //    without ordering, or different host threads) race on the array.
 //  - The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (host code cannot use the array's name as a device
-//    pointer); make that first call before any stream capture.
+//    pointer); make that first call before any stream capture.  A first
+//    call on a capturing stream returns UBG_ESTATE without touching the
+//    stream.
 //  - The work is enqueued on `stream` (NULL: the legacy default stream);
 //    the call returns once it is enqueued.
+#include <cmath>
 #include <mutex>
 
 #include "ubg_internal.cuh"
@@ -41,14 +45,24 @@ constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 void *g_scratch_ptr[kMaxDevices] = {};
 
+struct StateError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
 // Device address of the scratch array on the current device (set up once
-// per device, with that device current).
-void *scratch_address() {
+// per device, with that device current).  The set-up is refused while `st`
+// is capturing: it would end the caller's capture.
+void *scratch_address(cudaStream_t st) {
   int dev = 0;
   UBG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) throw ubg::ArgError("device index out of range");
   std::lock_guard<std::mutex> lock(g_scratch_mu);
   if (!g_scratch_ptr[dev]) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    UBG_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+      throw StateError("the first allocation-free solve on a device must not be made while its "
+                       "stream is capturing");
     void *ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || !ptr)
@@ -64,18 +78,20 @@ extern "C" int ubg_mg_solve_noalloc(float *p, int p_pitch, const float *f, int f
                                     const uint8_t *flag, int flag_pitch, int width, int height,
                                     float h, int zero_gradient_bc, void *stream) {
   using namespace ubg;
+  set_last_error("");
   try {
     if (!p || !f || !flag) throw ArgError("null argument");
     if (width < 8 || height < 8) throw ArgError("width and height must be >= 8");
     if (p_pitch < width || f_pitch < width || flag_pitch < width)
       throw ArgError("pitches must be at least the width");
+    if (!std::isfinite(h) || !(h > 0.0f)) throw ArgError("h must be finite and > 0");
     size_t need = mg_arena_bytes(width, height);
     if (need > kNoAllocScratchBytes)
       throw ArgError("grid " + std::to_string(width) + "x" + std::to_string(height) + " needs " +
                      std::to_string(need) + " bytes of solver scratch; the allocation-free solve "
                      "has " + std::to_string(kNoAllocScratchBytes) + " bytes");
     cudaStream_t st = (cudaStream_t)stream;
-    void *arena = scratch_address();
+    void *arena = scratch_address(st);
     MgHier mg;
     mg_bind(mg, width, height, h, arena, kNoAllocScratchBytes);
     MgLevel &L = mg.lv[0];
@@ -99,6 +115,12 @@ extern "C" int ubg_mg_solve_noalloc(float *p, int p_pitch, const float *f, int f
   } catch (const CudaError &e) {
     set_last_error(e.what());
     return UBG_ECUDA;
+  } catch (const StateError &e) {
+    set_last_error(e.what());
+    return UBG_ESTATE;
+  } catch (const std::bad_alloc &e) {
+    set_last_error("out of host memory");
+    return UBG_ENOMEM;
   } catch (const std::exception &e) {
     set_last_error(e.what());
     return UBG_ESTATE;

@@ -474,8 +474,8 @@ struct TracerArgs {
   float2 *points;       // ntracers x npoints ring of positions
   uint32_t *start, *end;
   float *ages;
-  const float2 *vxy;    // velocity texture, tw x th
-  int tw, th;
+  const float *vx, *vy;  // front velocity buffers (the texels are formed from them)
+  int P, W, H;
   const uint8_t *flag;  // cell flags, nfx x nfy, row pitch fpitch
   int nfx, nfy, fpitch;
   int ntracers, npoints;

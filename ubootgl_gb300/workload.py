@@ -159,3 +159,23 @@ def instance(W, H, seed, solid_range=(0.08, 0.15), u_in=None):
     flag = disc_flag(W, H, seed=seed + 1, solid_frac=frac)
     vx, vy = fast_velocity(flag, seed=seed + 2, u_in=u)
     return flag, vx, vy
+
+
+def seed_tracers(flag, ntr, npts, pdim, seed):
+    """ntr tracer heads uniform over the fluid cells (positions in [0, pdim]);
+    empty rings, ages uniform in [0, 2*pi) so that reseeding is spread out."""
+    H, W = flag.shape
+    rng = np.random.default_rng(seed)
+    pts = np.zeros((ntr, npts, 2), np.float32)
+    got = 0
+    while got < ntr:
+        n = 2 * (ntr - got)
+        x = rng.uniform(0.0, 1.0, n)
+        y = rng.uniform(0.0, 1.0, n)
+        ok = flag[np.minimum((y * H).astype(int), H - 1), np.minimum((x * W).astype(int), W - 1)] > 0
+        x, y = x[ok][:ntr - got], y[ok][:ntr - got]
+        pts[got:got + len(x), 0, 0] = x * pdim[0]
+        pts[got:got + len(x), 0, 1] = y * pdim[1]
+        got += len(x)
+    ages = rng.uniform(0.0, 6.28, ntr).astype(np.float32)
+    return pts, np.zeros(ntr, np.uint32), np.zeros(ntr, np.uint32), ages
