@@ -279,8 +279,10 @@ int ubg_selftest_div(const float *x, int n, float d, unsigned *mismatches);
  * (ubg_server_set_fuse_cells) per iteration, as one launch per kernel over
  * all of them, on a high-priority stream: a request joins at the next step
  * boundary and leaves after its last step.  Other sessions, and every
- * session in the stream mode, enqueue all their steps on their own stream
- * and the device overlaps the streams.  Either way a session's results are
+ * session in the stream mode, run on a pool of max_active host threads,
+ * each stepping one request on its session's own stream (a tolerance-mode
+ * solve waits on the device once per V-cycle there), and the device
+ * overlaps the streams.  Either way a session's results are
  * bit-identical to stepping it alone.  Latency = completion - submission. */
 typedef struct ubg_server ubg_server;
 typedef struct ubg_serve_stats {
@@ -292,7 +294,9 @@ typedef struct ubg_serve_stats {
   long long fused_steps;         /* fused launch sequences enqueued */
   long long fused_member_steps;  /* session steps they covered */
   double worker_fused_ms;        /* worker time spent enqueueing fused steps */
-  double worker_streams_ms;      /* worker time spent enqueueing stream requests */
+  double worker_streams_ms;      /* pool-thread time spent enqueueing stream requests */
+  int pending_sessions;          /* sessions waiting for device memory (UBG_ADMIT_QUEUE) */
+  long long admitted_from_queue; /* sessions admitted after waiting for memory */
 } ubg_serve_stats;
 int ubg_server_create(size_t budget_bytes, int max_active, ubg_server **out);
 int ubg_server_destroy(ubg_server *srv);
@@ -303,6 +307,15 @@ int ubg_server_set_mode(ubg_server *srv, int mode);
 /* The largest session (in cells) the fused mode steps fused (default 2^20);
  * larger sessions take their own stream. */
 int ubg_server_set_fuse_cells(ubg_server *srv, long long max_cells);
+#define UBG_ADMIT_REJECT 0 /* an open over budget fails with UBG_EBUSY (default) */
+#define UBG_ADMIT_QUEUE 1  /* it waits, in open order, until closes free the budget */
+/* Admission policy of later opens.  With UBG_ADMIT_QUEUE an open that does
+ * not fit returns UBG_OK and a session id at once; the inputs are kept in
+ * host memory and the session is built (in the thread of the ubg_server_close
+ * that frees the memory) when it reaches the front of the line and fits.
+ * Requests may be submitted to it meanwhile; they start once it is built.
+ * A session larger than the whole budget is still refused. */
+int ubg_server_set_admission(ubg_server *srv, int admission);
 /* Opens a session (Simulation(flag, pwidth, mu); vx / vy may be NULL, else
  * they initialise both buffers; opt may be NULL). */
 int ubg_server_open(ubg_server *srv, const float *flag, int width, int height, float pwidth,

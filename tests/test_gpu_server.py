@@ -126,3 +126,79 @@ def test_fused_many_sessions_match_plain_steps(lib, fuse_cells):
             assert np.array_equal(srv.get(sids[i], n), sim.get(n)), (W, n)
         sim.close()
     srv.close()
+
+
+def test_queue_admission_admits_after_close(lib):
+    """UBG_ADMIT_QUEUE: sessions over the budget wait instead of failing;
+    their requests start once a close frees memory, and the late session
+    steps exactly as if it had been admitted at once."""
+    from ubootgl_gb300 import _lib as L
+    from ubootgl_gb300.simulation import Server, Simulation
+    import ctypes as C
+    b = C.c_size_t()
+    L.check(lib.ubg_device_bytes(512, 256, C.byref(b)))
+    srv = Server(int(2.5 * b.value), max_active=2, admission="queue")
+    inputs = [session_inputs(512, 256, 70 + s) for s in range(4)]
+    ids = [srv.open(*x) for x in inputs]
+    assert all(i is not None for i in ids)
+    st = srv.stats()
+    assert st["sessions"] == 4 and st["pending_sessions"] == 2 and st["rejected_sessions"] == 0
+    reqs = [srv.submit(i, 3) for i in ids]
+    srv.wait(reqs[0])
+    srv.wait(reqs[1])
+    srv.drain()  # returns with the waiting sessions' requests still queued
+    st = srv.stats()
+    assert st["completed"] == 2 and st["queued"] == 2
+    srv.close_session(ids[0])  # frees memory: the first waiting session is built
+    srv.wait(reqs[2])
+    st = srv.stats()
+    assert st["admitted_from_queue"] == 1 and st["pending_sessions"] == 1
+    srv.close_session(ids[1])
+    srv.wait(reqs[3])
+    assert srv.stats()["admitted_from_queue"] == 2
+    for k in (2, 3):
+        sim = Simulation(inputs[k][0], 1.0, 1e-4)
+        for n, a in (("vx", inputs[k][1]), ("vy", inputs[k][2]), ("vx_back", inputs[k][1]),
+                     ("vy_back", inputs[k][2])):
+            sim.set(n, a)
+        for _ in range(3):
+            sim.step_cfl(0.5)
+        for n in ("vx", "vy", "p"):
+            assert np.array_equal(srv.get(ids[k], n), sim.get(n)), (k, n)
+        sim.close()
+    # a session larger than the whole budget is still refused
+    assert srv.open(*session_inputs(2048, 1024, 5)) is None
+    srv.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_tolerance_sessions_alone_vs_mixed(lib, precision):
+    """Tolerance-mode sessions run on the pool threads beside fused and
+    stream requests.  Their dot products accumulate with atomics, whose
+    order varies from run to run, so the result is reproducible to rounding,
+    not to the bit: the velocities alone and in the mix agree to 1e-5 of
+    max|v| (each projection solved to a relative residual of 1e-6)."""
+    from ubootgl_gb300.simulation import Server
+    target = session_inputs(384, 192, 91)
+    solo = Server(8 << 30, max_active=4)
+    sid = solo.open(*target, precision=precision, tol=1e-6)
+    for k in (2, 3):
+        solo.wait(solo.submit(sid, k))
+    alone = {n: solo.get(sid, n) for n in ("vx", "vy")}
+    solo.close()
+    mix = Server(8 << 30, max_active=4)
+    others = [mix.open(*session_inputs(W, H, 60 + i)) for i, (W, H) in
+              enumerate([(256, 128), (512, 256), (1024, 512)])]
+    others.append(mix.open(*session_inputs(256, 128, 65), tol=1e-6))
+    sid = mix.open(*target, precision=precision, tol=1e-6)
+    pending = []
+    for k in (2, 3):
+        for o in others:
+            pending.append(mix.submit(o, 3))
+        pending.append(mix.submit(sid, k))
+    for r in pending:
+        mix.wait(r)
+    for n in ("vx", "vy"):
+        a, b = mix.get(sid, n), alone[n]
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max(), n
+    mix.close()

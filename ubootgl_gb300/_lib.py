@@ -36,7 +36,8 @@ class ServeStats(C.Structure):
                 ("busy_ms", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("max_ms", C.c_double), ("fused_steps", C.c_longlong),
                 ("fused_member_steps", C.c_longlong), ("worker_fused_ms", C.c_double),
-                ("worker_streams_ms", C.c_double)]
+                ("worker_streams_ms", C.c_double), ("pending_sessions", C.c_int),
+                ("admitted_from_queue", C.c_longlong)]
 
 
 # name -> (restype, argtypes); every int-returning call is checked
@@ -79,6 +80,7 @@ _SIGS = {
     "ubg_server_destroy": (C.c_int, [_P]),
     "ubg_server_set_mode": (C.c_int, [_P, C.c_int]),
     "ubg_server_set_fuse_cells": (C.c_int, [_P, C.c_longlong]),
+    "ubg_server_set_admission": (C.c_int, [_P, C.c_int]),
     "ubg_server_open": (C.c_int, [_P, _FP, C.c_int, C.c_int, C.c_float, C.c_float, _FP, _FP,
                                   C.POINTER(Options), C.POINTER(C.c_int)]),
     "ubg_server_close": (C.c_int, [_P, C.c_int]),

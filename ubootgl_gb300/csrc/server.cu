@@ -2,20 +2,28 @@
 // sessions whose fields stay resident on the device.
 //
 // A session is one simulation handle (its own fields and stream).  Sessions
-// are admitted against a device-memory budget when they are opened.  A
-// request asks for k steps of one session.  The worker thread admits queued
-// requests in arrival order whenever a slot is free (one request in flight
-// per session; at most max_active stream requests and 4 * max_active fused
-// requests).  Requests of sessions that the fused form covers (FP32, fixed
+// are admitted against a device-memory budget when they are opened: over
+// budget, an open is refused (UBG_ADMIT_REJECT, the default) or the session
+// waits in FIFO order, with its inputs kept in host memory, until closed
+// sessions free enough budget (UBG_ADMIT_QUEUE).  A request asks for k steps
+// of one session.  The worker thread admits queued requests in arrival
+// order whenever a slot is free (one request in flight per session; at most
+// max_active stream requests and 4 * max_active fused requests; requests
+// of sessions still waiting for memory stay queued without blocking the
+// others).  Requests of sessions that the fused form covers (FP32, fixed
 // V-cycle count, at most 1M cells; see FusedStepper) are stepped together:
 // every worker iteration enqueues ONE step of every such request as one
 // launch per kernel over all of them, so a request that arrives joins at
 // the next step boundary and leaves after its k-th step (iteration-level
-// continuous batching, at most two steps in flight).  Other sessions (mixed
-// precision, tolerance mode, larger grids) enqueue their k steps on their
-// own stream.  The worker polls completion events.  Sessions touch only
-// their own memory and the fused step is bit-identical to stepping alone,
-// so a session's result does not depend on what else is in flight.
+// continuous batching, at most two steps in flight).  Other requests (mixed
+// precision, tolerance mode, larger grids, or every request in the stream
+// mode) go to a pool of max_active host threads, each of which runs one
+// request's steps on its session's own stream: the tolerance solver waits
+// on the device once per V-cycle, and a pool thread blocked there holds up
+// neither the worker nor the other sessions, whose work overlaps on the
+// device.  Sessions touch only their own memory and the fused step is
+// bit-identical to stepping alone, so a session's result does not depend on
+// what else is in flight.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -54,6 +62,13 @@ struct ubg_server {
     size_t bytes = 0;
     long long cells = 0;
     bool busy = false;
+    // waiting for device memory (queue admission): the inputs to build it
+    bool pending = false, building = false;
+    int width = 0, height = 0;
+    float pwidth = 1.0f, mu = 0.0f;
+    std::vector<float> flag, vx, vy;
+    bool has_opt = false;
+    ubg_options opt{};
   };
   struct Request {
     int session = 0;
@@ -62,8 +77,6 @@ struct ubg_server {
     double t_submit = 0, t_admit = 0, t_end = 0;
     bool fused = false;  // stepped by the fused stepper
     int remaining = 0;   // fused steps not yet enqueued
-    int enq = 0;         // stream steps enqueued so far
-    int chunks = 0;      // stream chunks enqueued so far
     bool finished = false;
     int error = 0;
   };
@@ -71,6 +84,12 @@ struct ubg_server {
   size_t budget = 0, used = 0;
   int max_active = 1;
   int mode = UBG_SERVE_FUSED;
+  int admission = UBG_ADMIT_REJECT;
+  std::deque<int> pending;  // sessions waiting for memory, in open order
+  long long admitted_from_queue = 0;
+  std::condition_variable cv_pool;
+  std::deque<uint64_t> stream_jobs;  // admitted stream requests for the pool
+  std::vector<std::thread> pool;
   long long fuse_max_cells = kFuseMaxCells;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -85,33 +104,74 @@ struct ubg_server {
   long long fused_steps = 0, fused_member_steps = 0;
   double worker_fused_ms = 0.0, worker_streams_ms = 0.0;
   double t_first = -1.0, t_last = 0.0;
-  bool stop = false;
+  bool stop = false, stop_pool = false;
   std::unique_ptr<FusedStepper> fs;
   std::thread worker;
 
-  // Enqueues the next chunk of a stream request's steps once at most one
-  // chunk is still queued (chunk i records evc[i % 2]).  Keeping only a few
-  // steps queued per session keeps the worker out of a full launch queue,
-  // where every launch would block it.
-  int stream_topup(Request &r, Session &s) {
-    if (r.enq >= r.steps) return UBG_OK;
-    if (r.chunks >= 2) {
-      cudaError_t q = cudaEventQuery(s.evc[r.chunks % 2]);
-      if (q == cudaErrorNotReady) return UBG_OK;
-      if (q != cudaSuccess) {
+  // Runs one stream request's steps on its session's stream, in chunks of
+  // kChunkSteps with at most two chunks queued (a full launch queue would
+  // block every launching thread, the worker's fused steps included), then
+  // waits for the last chunk.  Called by a pool thread without the lock.
+  int run_stream_request(Request &r, Session &s) {
+    int rc = UBG_OK;
+    int enq = 0, chunks = 0;
+    while (enq < r.steps && rc == UBG_OK) {
+      if (chunks >= 2 && cudaEventSynchronize(s.evc[chunks % 2]) != cudaSuccess) {
         cudaGetLastError();
         return UBG_ECUDA;
       }
+      const double t0 = now_ms();
+      const int n = std::min(kChunkSteps, r.steps - enq);
+      for (int k = 0; k < n && rc == UBG_OK; k++) rc = ubg_step_cfl(s.sim, r.cfl);
+      if (rc == UBG_OK && cudaEventRecord(s.evc[chunks % 2], s.st) != cudaSuccess) rc = UBG_ECUDA;
+      enq += n;
+      chunks++;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        worker_streams_ms += now_ms() - t0;
+      }
     }
-    const double t0 = now_ms();
-    const int n = std::min(kChunkSteps, r.steps - r.enq);
-    int rc = UBG_OK;
-    for (int k = 0; k < n && rc == UBG_OK; k++) rc = ubg_step_cfl(s.sim, r.cfl);
-    if (rc == UBG_OK && cudaEventRecord(s.evc[r.chunks % 2], s.st) != cudaSuccess) rc = UBG_ECUDA;
-    r.enq += n;
-    r.chunks++;
-    worker_streams_ms += now_ms() - t0;
+    if (rc == UBG_OK && chunks > 0 && cudaEventSynchronize(s.evc[(chunks - 1) % 2]) != cudaSuccess) {
+      cudaGetLastError();
+      rc = UBG_ECUDA;
+    }
     return rc;
+  }
+
+  // Pool thread: takes admitted stream requests until the server stops.
+  void pool_run() {
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+      cv_pool.wait(lk, [&] { return stop_pool || !stream_jobs.empty(); });
+      if (stream_jobs.empty()) return;
+      const uint64_t id = stream_jobs.front();
+      stream_jobs.pop_front();
+      Request &r = reqs[id];
+      Session &s = sessions[r.session];
+      lk.unlock();
+      const int rc = run_stream_request(r, s);
+      lk.lock();
+      finish(id, rc);
+      cv_work.notify_all();  // a slot is free
+    }
+  }
+
+  // Completion bookkeeping of an active request (lock held).
+  void finish(uint64_t id, int rc) {
+    Request &r = reqs[id];
+    Session &s = sessions[r.session];
+    r.t_end = now_ms();
+    r.finished = true;
+    r.error = rc;
+    s.busy = false;
+    if (rc == UBG_OK) {
+      latencies.push_back(r.t_end - r.t_submit);
+      cell_steps += s.cells * r.steps;
+      completed++;
+      t_last = r.t_end;
+    }
+    active.erase(std::remove(active.begin(), active.end(), id), active.end());
+    cv_done.notify_all();
   }
 
   void fail(Request &r, Session &s, int code) {
@@ -186,6 +246,10 @@ struct ubg_server {
           continue;
         }
         Session &s = sit->second;
+        if (s.pending) {  // still waiting for device memory
+          ++it;
+          continue;
+        }
         const bool fuse = mode == UBG_SERVE_FUSED && s.cells <= fuse_max_cells &&
                           FusedStepper::eligible(s.sim);
         if (s.busy || (fuse ? n_fused >= kFusedPerSlot * max_active : n_streams >= max_active)) {
@@ -208,7 +272,8 @@ struct ubg_server {
             rc = UBG_ECUDA;
           }
         } else {
-          rc = stream_topup(r, s);
+          stream_jobs.push_back(*it);
+          cv_pool.notify_one();
         }
         if (rc != UBG_OK) {
           fail(r, s, rc);
@@ -219,65 +284,53 @@ struct ubg_server {
         (fuse ? n_fused : n_streams)++;
         it = queue.erase(it);
       }
-      if (active.empty()) {
-        if (stop && queue.empty()) return;
-        cv_work.wait(lk);
+      bool fused_active = false;
+      for (uint64_t id : active) fused_active |= reqs[id].fused;
+      if (!fused_active) {
+        if (stop && queue.empty() && active.empty()) return;
+        // stream requests complete on the pool threads, which wake us
+        cv_work.wait_for(lk, std::chrono::milliseconds(50));
         continue;
       }
       bool stepped = fused_tick();
-      // stream top-ups and completion polling
+      // completion polling of the fused requests
       bool any = false;
       for (size_t i = 0; i < active.size();) {
-        Request &r = reqs[active[i]];
+        const uint64_t id = active[i];
+        Request &r = reqs[id];
         Session &s = sessions[r.session];
-        if (r.fused && r.remaining > 0) {
+        if (!r.fused || r.remaining > 0) {
           i++;
           continue;
         }
-        cudaError_t q = cudaSuccess;
-        if (!r.fused && r.enq < r.steps) {
-          const int c0 = r.chunks;
-          if (stream_topup(r, s) != UBG_OK) {
-            q = cudaErrorUnknown;
-          } else {
-            stepped |= r.chunks != c0;
-            i++;
-            continue;
-          }
-        } else {
-          // the request's last work: the stepper's event, or its last chunk
-          q = cudaEventQuery(r.fused ? s.evc[0] : s.evc[(r.chunks - 1) % 2]);
-          if (q == cudaErrorNotReady) {
-            i++;
-            continue;
-          }
+        // the request's last work: the stepper's event
+        cudaError_t q = cudaEventQuery(s.evc[0]);
+        if (q == cudaErrorNotReady) {
+          i++;
+          continue;
         }
-        r.t_end = now_ms();
-        r.finished = true;
+        int rc = UBG_OK;
         if (q != cudaSuccess) {
           cudaGetLastError();
-          r.error = UBG_ECUDA;
-        } else if (r.fused && fs->failed()) {
+          rc = UBG_ECUDA;
+        } else if (fs->failed()) {
           set_last_error("fused step: a launch found a table it was not made for");
-          r.error = UBG_ECUDA;
+          rc = UBG_ECUDA;
         }
-        s.busy = false;
-        latencies.push_back(r.t_end - r.t_submit);
-        cell_steps += s.cells * r.steps;
-        completed++;
-        t_last = r.t_end;
-        active.erase(active.begin() + i);
+        finish(id, rc);  // removes it from active
         any = true;
       }
-      if (any) {
-        cv_done.notify_all();
-      } else if (!stepped) {
+      if (!any && !stepped) {
         lk.unlock();
         std::this_thread::sleep_for(std::chrono::microseconds(20));
         lk.lock();
       }
     }
   }
+
+  // Builds the device state of waiting sessions in open order while the
+  // budget allows (called without the lock, after memory was freed).
+  void admit_pending();
 };
 
 namespace {
@@ -294,6 +347,7 @@ int ubg_server_create(size_t budget_bytes, int max_active, ubg_server **out) {
     s->budget = budget_bytes;
     s->max_active = max_active;
     s->worker = std::thread([s] { s->run(); });
+    for (int i = 0; i < max_active; i++) s->pool.emplace_back([s] { s->pool_run(); });
     *out = s;
   } catch (const std::exception &e) {
     return srv_fail(UBG_ESTATE, e.what());
@@ -310,10 +364,18 @@ int ubg_server_destroy(ubg_server *s) {
   }
   s->cv_work.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop_pool = true;
+  }
+  s->cv_pool.notify_all();
+  for (auto &t : s->pool)
+    if (t.joinable()) t.join();
   s->fs.reset();
   for (auto &kv : s->sessions) {
-    for (cudaEvent_t e : kv.second.evc) cudaEventDestroy(e);
-    ubg_destroy(kv.second.sim);
+    for (cudaEvent_t e : kv.second.evc)
+      if (e) cudaEventDestroy(e);
+    if (kv.second.sim) ubg_destroy(kv.second.sim);
   }
   delete s;
   set_last_error("");
@@ -335,57 +397,151 @@ int ubg_server_set_fuse_cells(ubg_server *s, long long max_cells) {
   return UBG_OK;
 }
 
-int ubg_server_open(ubg_server *s, const float *flag, int width, int height, float pwidth,
-                    float mu, const float *vx, const float *vy, const ubg_options *opt,
-                    int *session) {
-  if (!s || !flag || !session) return srv_fail(UBG_EINVAL, "null argument");
+int ubg_server_set_admission(ubg_server *s, int admission) {
+  if (!s || (admission != UBG_ADMIT_REJECT && admission != UBG_ADMIT_QUEUE))
+    return srv_fail(UBG_EINVAL, "bad argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->admission = admission;
+  return UBG_OK;
+}
+
+namespace {
+// Device bytes a session holds: the fields and hierarchy, plus the 16-bit
+// hierarchy of the fixed-mode mixed solver or the tolerance solver's arrays.
+size_t session_bytes(int width, int height, const ubg_options *opt, int *rc) {
   size_t bytes = 0;
-  int rc = ubg_device_bytes(width, height, &bytes);
-  if (rc) return rc;
-  if (opt && opt->precision != UBG_FP32)
-    bytes += (size_t)(3.0 * 2.0 * 4.0 / 3.0 * (double)((width + 31) / 32 * 32) * height) +
-             (size_t)((width + 31) / 32 * 32) * height * 4;
-  {
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->used + bytes > s->budget) {
-      s->rejected++;
-      return srv_fail(UBG_EBUSY, "device-memory budget exhausted: session not admitted");
-    }
-    s->used += bytes;  // reserved while the session is built
-  }
+  *rc = ubg_device_bytes(width, height, &bytes);
+  if (*rc) return 0;
+  const size_t P = (size_t)(width + 31) / 32 * 32;
+  if (opt && opt->solver_mode == UBG_SOLVE_TOLERANCE)
+    bytes += fcg_bytes(width, height, (int)P, opt->precision);
+  else if (opt && opt->precision != UBG_FP32)
+    bytes += (size_t)(3.0 * 2.0 * 4.0 / 3.0 * (double)P * height) + P * height * 4;
+  return bytes;
+}
+
+// Creates the session's simulation, uploads its inputs and makes its events.
+int build_session(ubg_server::Session &ses, const float *flag, const float *vx, const float *vy,
+                  const ubg_options *opt) {
   ubg_sim *sim = nullptr;
-  auto unreserve = [&] {
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->used -= bytes;
-  };
-  rc = ubg_create(flag, width, height, pwidth, mu, &sim);
+  int rc = ubg_create(flag, ses.width, ses.height, ses.pwidth, ses.mu, &sim);
   if (rc == UBG_OK && opt) rc = ubg_set_options(sim, opt);
   if (rc == UBG_OK && vx) rc = ubg_upload(sim, UBG_VX, vx);
   if (rc == UBG_OK && vx) rc = ubg_upload(sim, UBG_VX_BACK, vx);
   if (rc == UBG_OK && vy) rc = ubg_upload(sim, UBG_VY, vy);
   if (rc == UBG_OK && vy) rc = ubg_upload(sim, UBG_VY_BACK, vy);
-  ubg_server::Session ses;
-  if (rc == UBG_OK) {
-    void *st = nullptr;
-    ubg_stream(sim, &st);
-    ses.st = (cudaStream_t)st;
-    for (cudaEvent_t &e : ses.evc)
-      if (rc == UBG_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
-        cudaGetLastError();
-        rc = srv_fail(UBG_ECUDA, "event creation failed");
-      }
-  }
+  cudaEvent_t evc[2] = {nullptr, nullptr};
+  void *st = nullptr;
+  if (rc == UBG_OK) rc = ubg_stream(sim, &st);
+  for (cudaEvent_t &e : evc)
+    if (rc == UBG_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      rc = srv_fail(UBG_ECUDA, "event creation failed");
+    }
   if (rc != UBG_OK) {
-    for (cudaEvent_t e : ses.evc)
+    for (cudaEvent_t e : evc)
       if (e) cudaEventDestroy(e);
     if (sim) ubg_destroy(sim);
-    unreserve();
     return rc;
   }
   ses.sim = sim;
+  ses.st = (cudaStream_t)st;
+  ses.evc[0] = evc[0];
+  ses.evc[1] = evc[1];
+  return UBG_OK;
+}
+}  // namespace
+
+void ubg_server::admit_pending() {
+  for (;;) {
+    int id = 0;
+    ubg_server::Session inputs;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      if (pending.empty()) return;
+      id = pending.front();
+      Session &p = sessions[id];
+      if (used + p.bytes > budget) return;
+      used += p.bytes;  // reserved while the session is built
+      pending.pop_front();
+      inputs.width = p.width;
+      inputs.height = p.height;
+      inputs.pwidth = p.pwidth;
+      inputs.mu = p.mu;
+      inputs.flag.swap(p.flag);
+      inputs.vx.swap(p.vx);
+      inputs.vy.swap(p.vy);
+      inputs.has_opt = p.has_opt;
+      inputs.opt = p.opt;
+      p.building = true;
+    }
+    int rc = build_session(inputs, inputs.flag.data(), inputs.vx.empty() ? nullptr : inputs.vx.data(),
+                           inputs.vy.empty() ? nullptr : inputs.vy.data(),
+                           inputs.has_opt ? &inputs.opt : nullptr);
+    std::lock_guard<std::mutex> lk(mu);
+    Session &p = sessions[id];
+    if (rc != UBG_OK) {  // its queued requests fail with UBG_ESTATE
+      used -= p.bytes;
+      sessions.erase(id);
+    } else {
+      p.sim = inputs.sim;
+      p.st = inputs.st;
+      p.evc[0] = inputs.evc[0];
+      p.evc[1] = inputs.evc[1];
+      p.pending = false;
+      p.building = false;
+      admitted_from_queue++;
+    }
+    cv_work.notify_all();
+  }
+}
+
+int ubg_server_open(ubg_server *s, const float *flag, int width, int height, float pwidth,
+                    float mu, const float *vx, const float *vy, const ubg_options *opt,
+                    int *session) {
+  if (!s || !flag || !session) return srv_fail(UBG_EINVAL, "null argument");
+  int rc = UBG_OK;
+  const size_t bytes = session_bytes(width, height, opt, &rc);
+  if (rc) return rc;
+  ubg_server::Session ses;
+  ses.width = width;
+  ses.height = height;
+  ses.pwidth = pwidth;
+  ses.mu = mu;
   ses.bytes = bytes;
   ses.cells = (long long)width * height;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    const bool fits = s->used + bytes <= s->budget;
+    if (s->admission == UBG_ADMIT_QUEUE && bytes <= s->budget && (!fits || !s->pending.empty())) {
+      // wait in open order for memory: keep the inputs on the host
+      const size_t n = (size_t)width * height;
+      ses.pending = true;
+      ses.flag.assign(flag, flag + n);
+      if (vx) ses.vx.assign(vx, vx + (size_t)(width - 1) * height);
+      if (vy) ses.vy.assign(vy, vy + (size_t)width * (height - 1));
+      if (opt) {
+        ses.has_opt = true;
+        ses.opt = *opt;
+      }
+      *session = s->next_session++;
+      s->sessions[*session] = std::move(ses);
+      s->pending.push_back(*session);
+      set_last_error("");
+      return UBG_OK;
+    }
+    if (!fits) {
+      s->rejected++;
+      return srv_fail(UBG_EBUSY, "device-memory budget exhausted: session not admitted");
+    }
+    s->used += bytes;  // reserved while the session is built
+  }
+  rc = build_session(ses, flag, vx, vy, opt);
   std::lock_guard<std::mutex> lk(s->mu);
+  if (rc != UBG_OK) {
+    s->used -= bytes;
+    return rc;
+  }
   *session = s->next_session++;
   s->sessions[*session] = ses;
   return UBG_OK;
@@ -401,14 +557,25 @@ int ubg_server_close(ubg_server *s, int session) {
     bool queued = false;
     for (auto id : s->queue)
       if (s->reqs[id].session == session) queued = true;
-    if (it->second.busy || queued) return srv_fail(UBG_EBUSY, "session has requests in flight");
-    ses = it->second;
-    s->sessions.erase(it);
-    s->used -= ses.bytes;
+    if (it->second.building) return srv_fail(UBG_EBUSY, "session is being admitted");
+    if (it->second.pending) {
+      // never built: drop it from the waiting line (its queued requests
+      // fail with UBG_ESTATE)
+      s->pending.erase(std::remove(s->pending.begin(), s->pending.end(), session),
+                       s->pending.end());
+      s->sessions.erase(it);
+      s->cv_work.notify_all();
+    } else {
+      if (it->second.busy || queued) return srv_fail(UBG_EBUSY, "session has requests in flight");
+      ses = std::move(it->second);
+      s->sessions.erase(it);
+      s->used -= ses.bytes;
+    }
   }
   for (cudaEvent_t e : ses.evc)
     if (e) cudaEventDestroy(e);
-  ubg_destroy(ses.sim);
+  if (ses.sim) ubg_destroy(ses.sim);
+  s->admit_pending();  // freed memory may admit waiting sessions
   return UBG_OK;
 }
 
@@ -445,7 +612,16 @@ int ubg_server_wait(ubg_server *s, uint64_t request, double *latency_ms) {
 int ubg_server_drain(ubg_server *s) {
   if (!s) return srv_fail(UBG_EINVAL, "null handle");
   std::unique_lock<std::mutex> lk(s->mu);
-  s->cv_done.wait(lk, [&] { return s->queue.empty() && s->active.empty(); });
+  // every request of an admitted session done (requests of sessions still
+  // waiting for memory stay queued)
+  s->cv_done.wait(lk, [&] {
+    if (!s->active.empty()) return false;
+    for (uint64_t id : s->queue) {
+      auto it = s->sessions.find(s->reqs[id].session);
+      if (it != s->sessions.end() && !it->second.pending) return false;
+    }
+    return true;
+  });
   return UBG_OK;
 }
 
@@ -454,6 +630,7 @@ int ubg_server_session_sim(ubg_server *s, int session, ubg_sim **sim) {
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->sessions.find(session);
   if (it == s->sessions.end()) return srv_fail(UBG_EINVAL, "unknown session");
+  if (!it->second.sim) return srv_fail(UBG_ESTATE, "session still waiting for device memory");
   *sim = it->second.sim;
   return UBG_OK;
 }
@@ -474,6 +651,8 @@ int ubg_server_stats(ubg_server *s, ubg_serve_stats *out) {
   out->fused_member_steps = s->fused_member_steps;
   out->worker_fused_ms = s->worker_fused_ms;
   out->worker_streams_ms = s->worker_streams_ms;
+  out->pending_sessions = (int)s->pending.size();
+  out->admitted_from_queue = s->admitted_from_queue;
   if (!s->latencies.empty()) {
     std::vector<double> v = s->latencies;
     std::sort(v.begin(), v.end());

@@ -272,27 +272,37 @@ class Batch:
 class Server:
     """Step server over resident sessions (extension; ubg_server_*)."""
 
-    def __init__(self, budget_bytes, max_active=16, mode="fused", fuse_cells=None):
+    def __init__(self, budget_bytes, max_active=16, mode="fused", fuse_cells=None,
+                 admission="reject"):
         """mode "fused": one step of every in-flight FP32 request of at most
         `fuse_cells` cells (library default 2^20) per launch sequence
         (continuous batching); "streams": each request's steps on its
-        session's own stream."""
+        session's own stream.  admission "reject": an open over the memory
+        budget returns None; "queue": it waits for closes to free memory."""
         self._lib = L.load()
         h = C.c_void_p()
         L.check(self._lib.ubg_server_create(int(budget_bytes), int(max_active), C.byref(h)))
         self._h = h
         L.check(self._lib.ubg_server_set_mode(h, {"streams": 0, "fused": 1}[mode]))
+        L.check(self._lib.ubg_server_set_admission(h, {"reject": 0, "queue": 1}[admission]))
         if fuse_cells is not None:
             L.check(self._lib.ubg_server_set_fuse_cells(h, int(fuse_cells)))
 
-    def open(self, flag, vx=None, vy=None, pwidth=1.0, mu=1e-4, precision="fp32", vcycles=2):
-        """Returns the session id, or None when the memory budget rejects it."""
+    def open(self, flag, vx=None, vy=None, pwidth=1.0, mu=1e-4, precision="fp32", vcycles=2,
+             tol=None, max_vcycles=100):
+        """Returns the session id, or None when the memory budget rejects it.
+        tol: the tolerance solver (relative residual) instead of `vcycles`
+        fixed V-cycles."""
         flag = _f32(flag)
         H, W = flag.shape
         o = L.Options()
         L.check(self._lib.ubg_default_options(C.byref(o)))
         o.precision = {"fp32": L.FP32, "fp16": L.MIXED_FP16, "bf16": L.MIXED_BF16}[precision]
         o.vcycles = vcycles
+        if tol is not None:
+            o.solver_mode = L.SOLVE_TOLERANCE
+            o.tol = tol
+            o.max_vcycles = max_vcycles
         sid = C.c_int()
         rc = self._lib.ubg_server_open(
             self._h, L.fptr(flag), W, H, pwidth, mu,
