@@ -287,13 +287,15 @@ def run_ours(args):
         batched["fp32_small"] = batch_bench(L, lib, args.batch, args.batch_steps, args.warmup,
                                             "fp32", wmin=128, wmax=512)
     if args.serve_sessions > 0:
+        # the FP32 drop-in (two V-cycles), fused continuous batching: the
+        # specified 2000 req/s and a rate sweep
+        served["fixed_fp32_fused"] = serve_arm(L, args, "fp32", "fused", None,
+                                               [250, 500, 1000, 2000], spec_rate=args.serve_rate)
+        # the tolerance solver at the same divergence tolerance in FP32 and
+        # mixed precision (pool threads, one stream per request)
         for prec in args.serve_precisions.split(","):
-            for mode in args.serve_modes.split(","):
-                for rate, dur in ((args.serve_rate, args.serve_seconds),
-                                  (args.serve_rate_low, args.serve_seconds)):
-                    served["%s_%s_%g_per_s" % (prec, mode, rate)] = serve_bench(
-                        L, lib, args.serve_sessions, rate, dur, args.serve_budget_gb,
-                        args.serve_active, prec, mode)
+            served["tol_%s" % prec] = serve_arm(L, args, prec, "streams", args.serve_tol,
+                                                [25, 50, 100, 200, 400, 800])
 
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mcell-steps/s", "n_gpus": world,
@@ -473,15 +475,13 @@ def batch_bench(L, lib, n, steps, warmup, precision, seed=11, wmin=128, wmax=204
             "timing": "host wall clock, synchronised"}
 
 
-def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, precision, mode,
-                seed=5, wmin=256, wmax=4096, fuse_cells=None):
-    """Served stream: step requests arrive as a Poisson process (`rate` per
-    second for `duration` seconds) over n_sessions resident sessions with
-    widths log-uniform in [wmin, wmax] (height = width / 2), each asking for
-    k ~ U[1, 20] device-CFL steps; sessions admitted under a device-memory
-    budget.  Session fields are crops of one seeded 4096 x 2048 instance
-    (walls re-applied, own inflow speed).  mode: the server's stepping mode
-    ("fused" continuous batching or per-session "streams")."""
+def serve_open(L, n_sessions, budget_gb, max_active, precision, mode, tol=None, seed=5,
+               wmin=256, wmax=4096, fuse_cells=None):
+    """Opens n_sessions resident sessions, widths log-uniform in [wmin, wmax]
+    (height = width / 2) under a device-memory budget.  Session fields are
+    crops of one seeded 4096 x 2048 instance (walls re-applied, own inflow
+    speed); tol selects the tolerance solver.  Every session takes one
+    warm-up step."""
     from ubootgl_gb300 import workload as WL
     from ubootgl_gb300.simulation import Server
     rng = np.random.default_rng(seed)
@@ -489,6 +489,7 @@ def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, preci
     srv = Server(int(budget_gb * (1 << 30)), max_active=max_active, mode=mode,
                  fuse_cells=fuse_cells)
     ids, cells = [], {}
+    t0 = time.perf_counter()
     for W in WL.log_uniform_widths(n_sessions, wmin, wmax, seed + 1):
         H = W // 2
         flag = base_flag[:H, :W].copy()
@@ -501,17 +502,30 @@ def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, preci
         vx *= flag[:, :-1] * flag[:, 1:]
         vy *= flag[:-1, :] * flag[1:, :]
         vy[0, :] = 0.0
-        sid = srv.open(flag, vx, vy, precision=precision)
+        sid = srv.open(flag, vx, vy, precision=precision, tol=tol)
         if sid is not None:
             ids.append(sid)
             cells[sid] = W * H
-    rejected = srv.stats()["rejected_sessions"]
-    # warm every session once (graph capture, first-touch), outside the stream
     for r in [srv.submit(s, 1) for s in ids]:
         srv.wait(r)
-    srv2_base = srv.stats()
-    t = 0.0
-    arrivals = []
+    info = {"sessions": len(ids), "rejected_sessions": srv.stats()["rejected_sessions"],
+            "device_gb": round(srv.stats()["device_bytes_used"] / 2 ** 30, 2),
+            "budget_gb": budget_gb, "widths": [wmin, wmax], "max_active": max_active,
+            "precision": precision, "mode": mode,
+            "solver": ("tolerance, relative residual %g" % tol) if tol else "fixed, 2 V-cycles",
+            "open_s": round(time.perf_counter() - t0, 2)}
+    return srv, ids, cells, info
+
+
+def serve_point(srv, ids, cells, rate, duration, seed):
+    """Step requests arrive as a Poisson process (`rate` per second for
+    `duration` seconds), each for k ~ U[1, 20] device-CFL steps of a session
+    drawn uniformly; the run ends when every request has completed.
+    Sustained: everything completed within max(0.5 s, duration / 4) of the
+    last arrival window."""
+    rng = np.random.default_rng(seed)
+    base = srv.stats()
+    t, arrivals = 0.0, []
     while True:
         t += rng.exponential(1.0 / rate)
         if t > duration:
@@ -529,25 +543,42 @@ def serve_bench(L, lib, n_sessions, rate, duration, budget_gb, max_active, preci
     wall = time.perf_counter() - t0
     st = srv.stats()
     lat = np.array([srv.wait(r) for r in reqs]) if reqs else np.zeros(1)
-    srv.close()
-    done = st["completed"] - srv2_base["completed"]
-    cs = st["cell_steps"] - srv2_base["cell_steps"]
-    return {"sessions": len(ids), "rejected_sessions": rejected, "requests": len(arrivals),
-            "completed": done, "rate_per_s": rate, "duration_s": duration,
+    cs = st["cell_steps"] - base["cell_steps"]
+    return {"rate_per_s": rate, "duration_s": duration, "requests": len(arrivals),
+            "completed": st["completed"] - base["completed"],
             "p50_ms": round(float(np.percentile(lat, 50)), 3),
             "p99_ms": round(float(np.percentile(lat, 99)), 3),
             "max_ms": round(float(lat.max()), 3),
             "value": round(cs / wall / 1e6, 2), "unit": "Mcell-steps/s",
             "offered_mcell_steps_per_s": round(offered / 1e6, 1),
-            "device_gb": round(st["device_bytes_used"] / 2 ** 30, 2), "budget_gb": budget_gb,
-            "fused_steps": st["fused_steps"] - srv2_base["fused_steps"],
-            "fused_member_steps": st["fused_member_steps"] - srv2_base["fused_member_steps"],
-            "worker_ms": {"fused": round(st["worker_fused_ms"] - srv2_base["worker_fused_ms"], 1),
-                          "streams": round(st["worker_streams_ms"]
-                                           - srv2_base["worker_streams_ms"], 1)},
-            "widths": [wmin, wmax], "max_active": max_active, "precision": precision,
-            "mode": mode,
+            "sustained": bool(wall <= duration + max(0.5, duration / 4)),
+            "fused_steps": st["fused_steps"] - base["fused_steps"],
+            "fused_member_steps": st["fused_member_steps"] - base["fused_member_steps"],
             "wall_s": round(wall, 2)}
+
+
+def serve_arm(L, args, precision, mode, tol, rates, spec_rate=None):
+    """One served configuration: sessions opened once, then a sweep of request
+    rates (stopping at the first rate that is not sustained), plus the
+    specified rate if given.  Reports the highest sustained rate."""
+    srv, ids, cells, info = serve_open(L, args.serve_sessions, args.serve_budget_gb,
+                                       args.serve_active, precision, mode, tol)
+    sweep = []
+    for i, rate in enumerate(rates):
+        pt = serve_point(srv, ids, cells, rate, args.serve_seconds, seed=100 + i)
+        sweep.append(pt)
+        if not pt["sustained"]:
+            break
+    out = dict(info)
+    ok = [p for p in sweep if p["sustained"]]
+    out["max_sustained_rate_per_s"] = ok[-1]["rate_per_s"] if ok else None
+    out["at_max_sustained"] = ok[-1] if ok else None
+    out["sweep"] = sweep
+    if spec_rate is not None:
+        out["at_specified_rate"] = serve_point(srv, ids, cells, spec_rate, args.serve_seconds,
+                                               seed=99)
+    srv.close()
+    return out
 
 
 def replica_throughput(ms_local, cells, steps, world, pg, device):
@@ -817,17 +848,17 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-6,
                     help="relative residual of the tolerance modes")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--batch", type=int, default=64, help="batched instances (0: skip)")
+    ap.add_argument("--batch", type=int, default=256, help="batched instances (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--batch-precisions", default="fp32,fp16")
-    ap.add_argument("--serve-sessions", type=int, default=128, help="served sessions (0: skip)")
+    ap.add_argument("--serve-sessions", type=int, default=512, help="served sessions (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
-    ap.add_argument("--serve-rate-low", type=float, default=100.0)
-    ap.add_argument("--serve-seconds", type=float, default=1.5)
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-tol", type=float, default=1e-5,
+                    help="relative residual of the served tolerance-mode arms")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-active", type=int, default=32)
-    ap.add_argument("--serve-precisions", default="fp32")
-    ap.add_argument("--serve-modes", default="fused,streams")
+    ap.add_argument("--serve-precisions", default="fp32,fp16")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

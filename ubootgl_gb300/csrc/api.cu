@@ -1712,6 +1712,7 @@ void FusedStepper::leave(ubg_sim *s, cudaEvent_t ev) {
 // of one CUDA graph, so the members' kernels run concurrently and the host
 // issues one launch per batch step.
 struct ubg_batch {
+  static constexpr size_t kMaxBranches = 32;
   std::vector<ubg_sim *> sims;
   cudaStream_t st = nullptr;
   cudaEvent_t fork = nullptr, done = nullptr;
@@ -1952,6 +1953,21 @@ struct ubg_batch {
       if (!s->sinks.empty()) throw ArgError("a member has pending sinks (step it with ubg_step)");
       if (s->opt.solver_mode != UBG_SOLVE_FIXED) throw ArgError("batch steps need the fixed solver mode");
       if (s->prof) throw ArgError("a member is profiling");
+    }
+    {
+      // Many members and no fused launches (every member mixed-precision or
+      // large): one graph with a branch per member ran 256 members at 0.69x
+      // the members' own step graphs launched on their own streams
+      // (GB300), so past kMaxBranches each member launches its own graph.
+      std::vector<int> small, big;
+      if (!partition(device_dt, small, big) && sims.size() > kMaxBranches) {
+        for (size_t i = 0; i < sims.size(); i++)
+          sims[i]->step(device_dt ? 0.0f : dts[i], device_dt, cfl);
+        return;
+      }
+    }
+    for (size_t i = 0; i < sims.size(); i++) {
+      ubg_sim *s = sims[i];
       // work outside the graph, on the member's stream
       s->io_consume();
       bool accum = s->accum_dirty;

@@ -30,6 +30,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <type_traits>
 
 #define ALPHA_IS_ONE(a) ((a) == 1.0f)
@@ -1986,9 +1987,50 @@ double time_ms(EvPair &ev, cudaStream_t st, int warm, int reps, F &&f) {
 // coordinate descent over the tail size, then each tiled level's pre- and
 // post-smoothing tile.  The pressure is saved first and restored after the
 // trials (a V-cycle leaves p in the buffer it started in).
+// Tuning results by grid size: the choices depend on the level shapes, so
+// simulations of one size (the members of a batch, the sessions of a
+// server) share the first one's trials.
+struct TuneChoice {
+  int tail_cells = 0, tail_top = 0;
+  std::vector<int> pre, post;
+};
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, TuneChoice> g_tune_cache;
+
 void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
   init_kernel_attributes();
   const int nl = mg.levels;
+  const std::pair<int, int> key(mg.lv[0].w, mg.lv[0].h);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end() && (int)it->second.pre.size() == nl) {
+      mg.tail_cells = it->second.tail_cells;
+      mg.tail_top = it->second.tail_top;
+      for (int l = 0; l < nl; l++) {
+        mg.lv[l].tile_pre = it->second.pre[l];
+        mg.lv[l].tile_post = it->second.post[l];
+      }
+      if (report) {
+        char buf[160];
+        snprintf(buf, sizeof(buf),
+                 "{\"cached\": true, \"tail_cells\": %d, \"tail_top\": %d, \"levels\": [",
+                 mg.tail_cells, mg.tail_top);
+        std::string rep = buf;
+        const int last = (mg.tail_top >= 1 ? mg.tail_top : nl - 1) - 1;
+        for (int l = 0; l <= std::min(last, nl - 3); l++) {
+          const MgLevel &L = mg.lv[l];
+          snprintf(buf, sizeof(buf), "%s{\"level\": %d, \"w\": %d, \"h\": %d, \"pre\": \"%s\", \"post\": \"%s\"}",
+                   l ? ", " : "", l, L.w, L.h, L.tile_pre >= 0 ? kTileNames[L.tile_pre] : "default",
+                   L.tile_post >= 0 ? kTileNames[L.tile_post] : "default");
+          rep += buf;
+        }
+        rep += "]}";
+        *report += rep;
+      }
+      return;
+    }
+  }
   EvPair ev;
   MgLevel &L0 = mg.lv[0];
   const size_t pbytes = (size_t)L0.pitch * L0.h * sizeof(float);
@@ -2087,6 +2129,15 @@ void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
   }
   rep += "]}";
   if (report) *report += rep;
+  TuneChoice tc;
+  tc.tail_cells = mg.tail_cells;
+  tc.tail_top = mg.tail_top;
+  for (int l = 0; l < nl; l++) {
+    tc.pre.push_back(mg.lv[l].tile_pre);
+    tc.post.push_back(mg.lv[l].tile_post);
+  }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache[key] = tc;
 }
 
 void mg_low_alloc(MgLow &lo, const MgHier &mg, int prec) {
