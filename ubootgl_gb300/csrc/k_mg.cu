@@ -286,7 +286,9 @@ struct Tile {
 // (no bank conflicts).  Red = (x+y) odd; region parity equals global parity
 // because x0 + y0 is even.  After half sweep i only cells within HALO - i of
 // the tile are still exact, so each half sweep updates just that cone.
-template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S, class SC>
+// EXT: the tolerance hierarchy's rules (a.ext, a.scale_bits) compiled in;
+// the reference's path is built without them.
+template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S, class SC, bool EXT = false>
 __device__ __forceinline__ void k_mg_body(const MgArgsT<S, SC> &a, const int bx, const int by) {
   constexpr int NTY = NT / 32;
   using T = Tile<TX, TY, HALO>;
@@ -496,8 +498,8 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S, SC> &a, const int bx,
                    ((size_t)CW * CH * sizeof(SC) + 15) / 16 * 16;
     // correction scale of scaled 16-bit coarse levels (1 otherwise)
     float ecmul = 1.0f;
-    if (a.scale_bits) coarse_scale(a.scale_bits, a.scale_h1sq, a.scale_kexp, &ecmul);
-    const bool ext = a.ext != 0;
+    if (EXT && a.scale_bits) coarse_scale(a.scale_bits, a.scale_h1sq, a.scale_kexp, &ecmul);
+    const bool ext = EXT && a.ext != 0;
     // prolongate (pressure_solver.cpp:134-172); e * fine flag = e here.
     // Fine cell (rx, ry) = (2k + par, ry) lies over coarse column k of the
     // window and coarse row ry / 2; x parity is par and y parity ry & 1, both
@@ -554,7 +556,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S, SC> &a, const int bx,
                      ? 0.0f
                      : div_rn(((E0[j] + E1[j + 1]) + E0[j + 1]) + E1[j], a.wsum[k], a.rwsum[k]);
           }
-          if (a.scale_bits) pe = pe * ecmul;
+          if (EXT && a.scale_bits) pe = pe * ecmul;
           out[j] = out[j] + pe;
         }
         St::sts4(sp + row, make_float4(out[0], out[1], out[2], out[3]));
@@ -584,7 +586,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S, SC> &a, const int bx,
       if (ry < 0 || ry >= RY || rn < 0 || rn >= RY) continue;
       sp[IDX(rx, ry)] = sp[IDX(rx, rn)];
     }
-    if (a.ext && tid < 4) {  // corner cell <- its diagonal interior neighbour
+    if (EXT && a.ext && tid < 4) {  // corner cell <- its diagonal interior neighbour
       const int cxg = (tid & 1) ? w - 1 : 0, cyg = (tid & 2) ? h - 1 : 0;
       const int rx = cxg - x0, ry = cyg - y0;
       const int rnx = rx + ((tid & 1) ? -1 : 1), rny = ry + ((tid & 2) ? -1 : 1);
@@ -777,7 +779,7 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S, SC> &a, const int bx,
   if (a.rc) {
     const int cx0 = bx * (TX / 2), cy0 = by * (TY / 2);
     float rfac = a.rfac;
-    if (a.scale_bits) {
+    if (EXT && a.scale_bits) {
       float inv;
       rfac = rfac * (coarse_scale(a.scale_bits, a.scale_h1sq, a.scale_kexp, &inv) * a.scale_h1sq);
     }
@@ -852,11 +854,12 @@ __device__ __forceinline__ void k_mg_body(const MgArgsT<S, SC> &a, const int bx,
   }
 }
 
-template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float, class SC = S>
+template <int TX, int TY, int HALO, bool ALPHA1, int NT, class S = float, class SC = S,
+          bool EXT = false>
 __global__ void __launch_bounds__(NT, NT >= 1024 ? 1 : (NT == 512 ? 2 : 4))
     k_mg(MgArgsT<S, SC> a) {
   griddep_wait();
-  k_mg_body<TX, TY, HALO, ALPHA1, NT, S, SC>(a, blockIdx.x, blockIdx.y);
+  k_mg_body<TX, TY, HALO, ALPHA1, NT, S, SC, EXT>(a, blockIdx.x, blockIdx.y);
 }
 // One launch over the members of a batch (FP32): block -> member -> tile.
 template <int TX, int TY, int HALO, bool ALPHA1, int NT>
@@ -1175,24 +1178,43 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1)
 }
 
 // ------------------------------------------------------------ launches
+// The tiles the tolerance hierarchy uses (chosen by level width): the only
+// ones built with its rules.
+template <int TX, int TY, int HALO, bool A1>
+constexpr bool ext_tile() {
+  return A1 && HALO == 8 && ((TX == 112 && TY == 50) || (TX == 48 && TY == 16));
+}
+
 template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float, class SC = S>
 void launch_mg_t(const MgArgsT<S, SC> &a, cudaStream_t st) {
   using T = Tile<TX, TY, HALO>;
   dim3 grid((a.w + TX - 1) / TX, (a.h + TY - 1) / TY);
-  launch_pdl(k_mg<TX, TY, HALO, A1, NT, S, SC>, grid, dim3(32, NT / 32),
-             T::smem(sizeof(S), sizeof(SC)), st, a);
+  if (a.ext) {
+    if constexpr (ext_tile<TX, TY, HALO, A1>()) {
+      launch_pdl(k_mg<TX, TY, HALO, A1, NT, S, SC, true>, grid, dim3(32, NT / 32),
+                 T::smem(sizeof(S), sizeof(SC)), st, a);
+    } else {
+      throw ArgError("tolerance hierarchy: tile not built with its rules");
+    }
+  } else if constexpr (std::is_same<S, SC>::value) {
+    launch_pdl(k_mg<TX, TY, HALO, A1, NT, S, SC, false>, grid, dim3(32, NT / 32),
+               T::smem(sizeof(S), sizeof(SC)), st, a);
+  } else {
+    throw ArgError("mixed storage types only in the tolerance hierarchy");
+  }
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }
 
-template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float, class SC = S>
+template <int TX, int TY, int HALO, bool A1, int NT = 256, class S = float, class SC = S,
+          bool EXT = false>
 void set_smem_attr() {
-  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S, SC>,
+  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S, SC, EXT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)Tile<TX, TY, HALO>::smem(sizeof(S), sizeof(SC))));
   // one carveout for every kernel of a V-cycle: no L1 / shared-memory
   // reconfiguration between consecutive launches
-  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S, SC>,
+  UBG_CUDA(cudaFuncSetAttribute(k_mg<TX, TY, HALO, A1, NT, S, SC, EXT>,
                                 cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 }
 
@@ -1243,12 +1265,19 @@ static void set_all_kernel_attributes() {
   set_vcycle_attrs<__nv_bfloat16>();
   set_tail_attr<__half, double>();
   set_tail_attr<__nv_bfloat16, double>();
-  // the tolerance solver: FP32 level 0 over 16-bit coarse levels, FP32
-  // arithmetic in the tail over 16-bit storage
-  set_smem_attr<112, 50, 8, true, 512, float, __half>();
-  set_smem_attr<48, 16, 8, true, 256, float, __half>();
-  set_smem_attr<112, 50, 8, true, 512, float, __nv_bfloat16>();
-  set_smem_attr<48, 16, 8, true, 256, float, __nv_bfloat16>();
+  // the tolerance solver: its rules on the width-chosen tiles, FP32 level 0
+  // over 16-bit coarse levels, FP32 arithmetic in the tail over 16-bit
+  // storage
+  set_smem_attr<112, 50, 8, true, 512, float, float, true>();
+  set_smem_attr<48, 16, 8, true, 256, float, float, true>();
+  set_smem_attr<112, 50, 8, true, 512, __half, __half, true>();
+  set_smem_attr<48, 16, 8, true, 256, __half, __half, true>();
+  set_smem_attr<112, 50, 8, true, 512, __nv_bfloat16, __nv_bfloat16, true>();
+  set_smem_attr<48, 16, 8, true, 256, __nv_bfloat16, __nv_bfloat16, true>();
+  set_smem_attr<112, 50, 8, true, 512, float, __half, true>();
+  set_smem_attr<48, 16, 8, true, 256, float, __half, true>();
+  set_smem_attr<112, 50, 8, true, 512, float, __nv_bfloat16, true>();
+  set_smem_attr<48, 16, 8, true, 256, float, __nv_bfloat16, true>();
   set_tail_attr<__half, float>();
   set_tail_attr<__nv_bfloat16, float>();
 }
