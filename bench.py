@@ -364,9 +364,20 @@ def time_tolerance(L, lib, flag, vx, vy, precision, steps, warmup, dev, tol):
     sim.sync()
     ms = e0.elapsed_time(e1)
     finite = bool(np.isfinite(sim.get("p")).all())
+    # per kernel class (direct launches with event pairs), a few steps
+    sim.profile(True)
+    sim.profile_reset()
+    nprof = 3
+    for _ in range(nprof):
+        sim.step_cfl(0.5)
+    sim.sync()
+    classes = sim.profile_classes()
+    sim.profile(False)
     sim.close()
+    kern = {k: {"ms_per_step": round(v[0] / nprof, 4), "launches_per_step": round(v[1] / nprof, 1)}
+            for k, v in sorted(classes.items(), key=lambda kv: -kv[1][0])}
     return {"value": round(W * H * steps / (ms / 1e3) / 1e6, 2), "unit": "Mcell-steps/s",
-            "ms_per_step": round(ms / steps, 4), "steps": steps, "tol": tol,
+            "ms_per_step": round(ms / steps, 4), "steps": steps, "tol": tol, "kernels": kern,
             "vcycles_per_projection": round(float(np.mean(cycles)), 2),
             "vcycles_max": int(max(cycles)), "residual_max": float("%.3e" % max(rels)),
             "solver": "flexible CG (FP64 pressure, FP32 vectors, FP64 norms) preconditioned by "

@@ -318,7 +318,7 @@ struct ubg_sim {
   // The gradient kernel also starts the max|u| reduction for the next CFL dt.
   // Tolerance mode (extension): flexible CG preconditioned by the tolerance
   // hierarchy's V-cycle (k_krylov.cu) until ||r|| <= tol ||f_c||; the
-  // gradient update reads its FP64 pressure.
+  // gradient update reads its double-float pressure.
   void project(int nsink_cells) {
     launch_divergence(v, fx, fy, f(), d_sc, st);
     launch_sinks(f(), P, d_sinks, nsink_cells, st);
@@ -328,7 +328,7 @@ struct ubg_sim {
       last_vcycles = fcg_solve(fcg, flag(), f(), p(), (double)opt.tol, opt.max_vcycles, &last_rel, st);
       launch_pbc(p(), P, W, H, bc, st);
       UBG_CUDA(cudaMemsetAsync(d_umax, 0, sizeof(unsigned int), st));
-      launch_gradient64(v, fx, fy, fcg.x, d_sc, d_umax, st);
+      launch_gradient_df(v, fx, fy, fcg.xh, fcg.xl, d_sc, d_umax, st);
       return;
     }
     solve_pressure();

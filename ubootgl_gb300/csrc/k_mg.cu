@@ -2622,7 +2622,7 @@ void ext_hier_alloc(MgHier &mg, int W, int H, float h0) {
   mg.norm = (double *)p;
   mg.post_norm2 = nullptr;
   mg.ext = true;
-  mg.ncoarse = 40;
+  mg.ncoarse = 16;
   mg.lv = lv;
   mg.levels = (int)lv.size();
   mg.tail_top = choose_tail(lv, 4096, 4, mg.levels - 1);

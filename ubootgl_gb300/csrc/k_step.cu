@@ -15,7 +15,7 @@ const char *kernel_class_name(int kc) {
   static const char *n[KC_COUNT] = {"vbc", "accum", "diffuse", "advect", "divergence", "sinks",
                                     "pbc", "gradient", "cfl", "smooth_l0", "smooth_coarse",
                                     "resid_restrict_l0", "resid_restrict_coarse", "coarsen",
-                                    "residual", "tracers", "other", "smooth_l1", "tail"};
+                                    "residual", "tracers", "other", "smooth_l1", "tail", "krylov"};
   return (kc >= 0 && kc < KC_COUNT) ? n[kc] : "?";
 }
 

@@ -442,13 +442,23 @@ struct FcgScalars {
   unsigned pad;
 };
 
+// Per-block partial sums of the Krylov reductions (summed in block order by
+// the last block of each launch) and the ticket that finds that block.
+constexpr int kFcgMaxBlocks = 2048;
+struct FcgPartials {
+  double v[kFcgMaxBlocks][4];
+  unsigned m[kFcgMaxBlocks];
+  unsigned ticket;
+};
+
 struct FcgSolver {
   MgHier mg;  // the tolerance hierarchy (level 0: rhs = r, e = z)
   MgLow lo;   // its 16-bit arrays (mixed precision)
   int prec = UBG_FP32;
-  double *x = nullptr;  // FP64 pressure iterate, W x H pitched like the fields
+  float *xh = nullptr, *xl = nullptr;  // double-float pressure iterate, pitched like the fields
   float *d[2] = {nullptr, nullptr}, *q = nullptr;
   FcgScalars *dev = nullptr, *host = nullptr;
+  FcgPartials *part = nullptr;  // zeroed at allocation (ticket 0)
   void *arena = nullptr;
   bool dirty = true;  // the flag changed since the coarse flags were built
   int W = 0, H = 0, P = 0;
@@ -459,15 +469,15 @@ void fcg_free(FcgSolver &fs);
 size_t fcg_bytes(int W, int H, int P, int prec);
 void fcg_set_precision(FcgSolver &fs, int prec);
 // Solves the zero-gradient system for p (warm start: p as given; result:
-// p's interior cells, and fs.x in FP64) until ||r|| <= tol ||f_c||, at most
+// p's interior cells, and fs.xh + fs.xl as a double-float) until ||r|| <= tol ||f_c||, at most
 // max_iter iterations (one V-cycle each).  Synchronises once per
 // iteration.  Returns the iterations run; *rel = ||f_c + L x|| / ||f_c||
 // of the final x.
 int fcg_solve(FcgSolver &fs, const uint8_t *flag, const float *f, float *p, double tol,
               int max_iter, double *rel, cudaStream_t st);
-// The pressure-gradient update from the FP64 pressure x.
-void launch_gradient64(const VelBufs &v, int fx, int fy, const double *x, const StepScalars *sc,
-                       unsigned *umax_bits, cudaStream_t st);
+// The pressure-gradient update from the double-float pressure xh + xl.
+void launch_gradient_df(const VelBufs &v, int fx, int fy, const float *xh, const float *xl,
+                        const StepScalars *sc, unsigned *umax_bits, cudaStream_t st);
 
 // ------------------------------------------------------------- tracers
 struct TracerArgs {
@@ -501,7 +511,7 @@ extern thread_local LaunchStats g_stats;
 enum KernelClass {
   KC_VBC = 0, KC_ACCUM, KC_DIFFUSE, KC_ADVECT, KC_DIVERGENCE, KC_SINKS, KC_PBC, KC_GRADIENT,
   KC_CFL, KC_SMOOTH_L0, KC_SMOOTH_COARSE, KC_RESTRICT_L0, KC_RESTRICT_COARSE, KC_COARSEN,
-  KC_RESIDUAL, KC_TRACERS, KC_OTHER, KC_SMOOTH_L1, KC_TAIL, KC_COUNT
+  KC_RESIDUAL, KC_TRACERS, KC_OTHER, KC_SMOOTH_L1, KC_TAIL, KC_KRYLOV, KC_COUNT
 };
 const char *kernel_class_name(int kc);
 

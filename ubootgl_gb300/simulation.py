@@ -210,7 +210,7 @@ class Simulation:
     def profile_classes(self):
         """{kernel class: (total ms, launches)} accumulated while profiling."""
         out = {}
-        for kc in range(19):
+        for kc in range(20):
             name, ms, n = C.c_char_p(), C.c_double(), C.c_int()
             L.check(self._lib.ubg_profile_class(self._h, kc, C.byref(name), C.byref(ms),
                                                 C.byref(n)))
