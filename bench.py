@@ -718,12 +718,15 @@ def scale_bench(L, lib, steps, warmup, dev, W=8192, H=4096, ntr=1 << 20, npts=30
     inside = float(np.mean((heads[:, 0] >= 0) & (heads[:, 0] <= pdim[0]) &
                            (heads[:, 1] >= 0) & (heads[:, 1] <= pdim[1])))
     del tr
-    # the tolerance solver's V-cycles to 1e-6 at this size (3 steps)
-    sim.set_options(solver_mode=L.SOLVE_TOLERANCE, tol=1e-6, max_vcycles=200)
-    tol_cycles = []
-    for _ in range(3):
-        sim.step_cfl(0.5)
-        tol_cycles.append(sim.solver_stats())
+    # the tolerance solver's V-cycles to 1e-6 at this size (3 steps per
+    # precision of the coarse levels)
+    tol_cycles = {}
+    for prec in ("fp32", "fp16"):
+        sim.set_options(solver_mode=L.SOLVE_TOLERANCE, tol=1e-6, max_vcycles=200, precision=prec)
+        tol_cycles[prec] = []
+        for _ in range(3):
+            sim.step_cfl(0.5)
+            tol_cycles[prec].append(sim.solver_stats())
     sim.close()
     return {"workload": "fluid step %dx%d, 400 discs r 20-60 cells (%.1f %% solid), FP32, "
                         "2 V-cycles, dt=0.5h/max|u|, + %d tracers x %d points"
@@ -735,7 +738,7 @@ def scale_bench(L, lib, steps, warmup, dev, W=8192, H=4096, ntr=1 << 20, npts=30
             "tracer_alg_bytes": "36 B per tracer (positions r/w, ring pointers, age) plus the "
                                 "velocity / flag gathers",
             "vcycles_per_projection": vcycles, "tolerance_vcycles_to_1e-6":
-                [[c, float("%.2e" % r)] for c, r in tol_cycles],
+                {k: [[c, float("%.2e" % r)] for c, r in v] for k, v in tol_cycles.items()},
             "kernels": kern, "fields_finite": finite, "tracer_heads_inside": round(inside, 4)}
 
 

@@ -304,12 +304,55 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_resid(const float *__restrict__ 
   block_reduce<2>(v, mx, dst, &sc->maxbits, pr);
 }
 
-// zq = (z, q_prev); zeroes the accumulators of k_fcg_dir.
+// Sum of z over the interior fluid cells.  A maps a constant on a fluid
+// region to 0, so nothing in the iteration removes the constant that the
+// V-cycle leaves in z (its coarsest level is singular, and its right-hand
+// side sums to zero only up to rounding).  Carried into the direction d,
+// that constant enters (z, q), (d, q) and (d, r) through the rounding of
+// sum(q) and sum(r) over the region; once the constant dominates d, those
+// dot products are rounding noise and the iteration diverges from the
+// accuracy it had reached (at 8192 x 4096 with 400 discs the residual
+// climbed from 1e-6 to 1e-3).  k_fcg_zq and k_fcg_dir subtract the mean.
+__global__ void __launch_bounds__(BX *BY) k_fcg_zsum(const float *__restrict__ z,
+                                                     const uint8_t *__restrict__ code, int W,
+                                                     int H, int P, FcgScalars *sc,
+                                                     FcgPartials *pr) {
+  griddep_wait();
+  float s = 0.0f;
+  const int tiles_x = (W + 4 * BX - 1) / (4 * BX), ntiles = tiles_x * ((H + BY - 1) / BY);
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int x4 = ((t % tiles_x) * BX + threadIdx.x) * 4, y = (t / tiles_x) * BY + threadIdx.y;
+    if (x4 >= W || y < 1 || y >= H - 1) continue;
+    const size_t i = (size_t)y * P + x4;
+    if (x4 >= 1 && x4 + 4 <= W - 1) {
+      const float4 a = *reinterpret_cast<const float4 *>(z + i);
+      const uchar4 c = __ldg(reinterpret_cast<const uchar4 *>(code + i));
+      s = s + ((((c.x & 1u) ? a.x : 0.0f) + ((c.y & 1u) ? a.y : 0.0f)) +
+               (((c.z & 1u) ? a.z : 0.0f) + ((c.w & 1u) ? a.w : 0.0f)));
+    } else {
+      for (int j = 0; j < 4; j++) {
+        const int x = x4 + j;
+        if (x >= 1 && x < W - 1 && (__ldg(code + i + j) & 1u)) s = s + z[i + j];
+      }
+    }
+  }
+  double v[1] = {(double)s};
+  double *const dst[1] = {&sc->zsum};
+  block_reduce<1>(v, 0u, dst, nullptr, pr);
+}
+
+__device__ __forceinline__ float z_mean(const FcgScalars *sc) {
+  return sc->nfluid > 0.0 ? (float)(sc->zsum / sc->nfluid) : 0.0f;
+}
+
+// zq = (z - zm, q_prev), zm the mean of z over the interior fluid cells;
+// zeroes the accumulators of k_fcg_dir.
 __global__ void __launch_bounds__(BX *BY) k_fcg_zq(const float *__restrict__ z,
                                                    const float *__restrict__ q, int W, int H,
                                                    int P, FcgScalars *sc, int slot,
                                                    FcgPartials *pr) {
   griddep_wait();
+  const float zm = z_mean(sc);
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     sc->dq[slot] = 0.0;
     sc->dr = 0.0;
@@ -325,7 +368,7 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_zq(const float *__restrict__ z,
       const float4 a = *reinterpret_cast<const float4 *>(z + i);
       const float4 b = *reinterpret_cast<const float4 *>(q + i);
       // q is 0 outside the interior fluid cells and beyond the width
-      s = s + (((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w);
+      s = s + ((((a.x - zm) * b.x + (a.y - zm) * b.y) + (a.z - zm) * b.z) + (a.w - zm) * b.w);
     }
   }
   double v[1] = {(double)s};
@@ -333,10 +376,13 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_zq(const float *__restrict__ z,
   block_reduce<1>(v, 0u, dst, nullptr, pr);
 }
 
-// d = z + beta d_old (beta = -zq / dq_prev; 0 on the first iteration) on
-// every cell, q = A d = -ihsq * sum_n flag_n (d_n - d) on the interior
-// fluid cells (0 elsewhere), (d, q) and (d, r); zeroes the accumulators of
-// k_fcg_update.
+// d = (z - zm) + beta d_old (beta = -zq / dq_prev; 0 on the first
+// iteration) on the interior fluid cells and the edges, d = 0 on the
+// interior solid cells (where z and d_old are 0), q = A d = -ihsq * sum_n
+// flag_n (d_n - d) on the interior fluid cells (0 elsewhere), (d, q) and
+// (d, r); zeroes the accumulators of k_fcg_update.  The shift by zm is
+// applied to every value read, so q sees the stored d of each fluid cell;
+// the values of solid neighbours never enter q.
 __global__ void __launch_bounds__(BX *BY) k_fcg_dir(const float *__restrict__ z,
                                                     const float *__restrict__ dold, float *dnew,
                                                     float *q, const float *__restrict__ r,
@@ -345,6 +391,7 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_dir(const float *__restrict__ z,
                                                     int first, int slot, FcgPartials *pr) {
   griddep_wait();
   const float beta = first ? 0.0f : (float)(-sc->zq / sc->dq[slot ^ 1]);
+  const float zm = z_mean(sc);
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     sc->rr = 0.0;
     sc->maxbits = 0u;
@@ -356,17 +403,19 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_dir(const float *__restrict__ z,
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int x4 = ((t % tiles_x) * BX + threadIdx.x) * 4, y = (t / tiles_x) * BY + threadIdx.y;
     if (x4 < W && y < H) {
-      auto D = [&](size_t i) { return first ? __ldg(z + i) : __ldg(z + i) + beta * __ldg(dold + i); };
+      auto D = [&](size_t i) {
+        return first ? __ldg(z + i) - zm : (__ldg(z + i) - zm) + beta * __ldg(dold + i);
+      };
       const size_t i0 = (size_t)y * P + x4;
       float dc[4], qv[4] = {0.f, 0.f, 0.f, 0.f};
       if (x4 >= 2 && x4 + 4 <= W - 2 && y >= 2 && y <= H - 3) {
         // interior: every neighbour is an interior cell; rows as float4
         auto D4 = [&](size_t i, float *o) {
           const float4 a = __ldg(reinterpret_cast<const float4 *>(z + i));
-          o[0] = a.x;
-          o[1] = a.y;
-          o[2] = a.z;
-          o[3] = a.w;
+          o[0] = a.x - zm;
+          o[1] = a.y - zm;
+          o[2] = a.z - zm;
+          o[3] = a.w - zm;
           if (!first) {
             const float4 b = __ldg(reinterpret_cast<const float4 *>(dold + i));
             o[0] = o[0] + beta * b.x;
@@ -396,6 +445,9 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_dir(const float *__restrict__ z,
           dq = __fmaf_rn(dc[j], qv[j], dq);
           dr = __fmaf_rn(dc[j], R4[j], dr);
         }
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (!(C4[j] & 1u)) dc[j] = 0.0f;
       } else {
 #pragma unroll
         for (int j = 0; j < 4; j++) dc[j] = (x4 + j < W) ? D(i0 + j) : 0.0f;
@@ -414,6 +466,9 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_dir(const float *__restrict__ z,
           dq = __fmaf_rn(dc[j], qv[j], dq);
           dr = __fmaf_rn(dc[j], __ldg(r + i), dr);
         }
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (x4 + j < W && interior(x4 + j, y, W, H) && !(__ldg(code + i0 + j) & 1u)) dc[j] = 0.0f;
       }
       if (x4 + 3 < W) {
         *reinterpret_cast<float4 *>(dnew + i0) = make_float4(dc[0], dc[1], dc[2], dc[3]);
@@ -677,6 +732,7 @@ int fcg_solve(FcgSolver &fs, const uint8_t *flag, const float *f, float *p, doub
     return dim3((unsigned)std::min<long long>(n, kFcgMaxBlocks));
   };
   const dim3 g_fsum = wave(k_fcg_fsum), g_resid = wave(k_fcg_resid), g_zq = wave(k_fcg_zq),
+             g_zsum = wave(k_fcg_zsum),
              g_dir = wave(k_fcg_dir), g_update = wave(k_fcg_update);
   float *r = L0.rhs;  // the V-cycle's level-0 right-hand side is the residual
   UBG_CUDA(cudaMemsetAsync(fs.dev, 0, sizeof(FcgScalars), st));
@@ -709,7 +765,13 @@ int fcg_solve(FcgSolver &fs, const uint8_t *flag, const float *f, float *p, doub
   // replacement that finds the residual not at least halved since the last
   // one ends the solve: the tolerance is below what the FP32 vectors
   // resolve.
+  // A solve that ends above the residual it started from (the iteration
+  // diverged: 16-bit coarse levels too coarse in precision for the grid,
+  // BF16 at 8192 x 4096) keeps its starting pressure instead; a recurrence
+  // residual 100 times the starting one ends it early.
   double rr = fs.host->rr, last_true = rr;
+  const double start_rr = rr;
+  bool diverged = false;
   bool fresh = true, first = true;
   int it = 0, cur_d = 0;
   auto replace_residual = [&]() {
@@ -743,6 +805,12 @@ int fcg_solve(FcgSolver &fs, const uint8_t *flag, const float *f, float *p, doub
     ext_vcycle(mg, fs.prec == UBG_FP32 ? nullptr : &fs.lo, fs.prec, &fs.dev->maxbits, st);
     const float *z = L0.e[mg.cur0];
     const int slot = it & 1;
+    {
+      ProfScope ps_(KC_KRYLOV, st);
+      k_fcg_zsum<<<g_zsum, blk, 0, st>>>(z, L0.code, W, H, P, fs.dev, fs.part);
+    }
+    UBG_LAUNCH_CHECK();
+    g_stats.launches++;
     if (it > 0) {  // (also zeroes the accumulators of k_fcg_dir)
       {
         ProfScope ps_(KC_KRYLOV, st);
@@ -770,13 +838,27 @@ int fcg_solve(FcgSolver &fs, const uint8_t *flag, const float *f, float *p, doub
     fresh = false;
     read();
     rr = fs.host->rr;
+    if (rr > 1.0e4 * start_rr) {
+      diverged = true;
+      break;
+    }
   }
-  {
-    ProfScope ps_(KC_KRYLOV, st);
-    k_fcg_store<<<grid, blk, 0, st>>>(fs.xh, fs.xl, p, W, H, P);
+  if (diverged || rr > start_rr) {
+    {
+      ProfScope ps_(KC_KRYLOV, st);
+      k_fcg_load<<<grid, blk, 0, st>>>(p, fs.xh, fs.xl, W, H, P);
+    }
+    UBG_LAUNCH_CHECK();
+    g_stats.launches++;
+    rr = start_rr;
+  } else {
+    {
+      ProfScope ps_(KC_KRYLOV, st);
+      k_fcg_store<<<grid, blk, 0, st>>>(fs.xh, fs.xl, p, W, H, P);
+    }
+    UBG_LAUNCH_CHECK();
+    g_stats.launches++;
   }
-  UBG_LAUNCH_CHECK();
-  g_stats.launches++;
   if (rel) *rel = std::sqrt(rr / (ff > 0.0 ? ff : 1.0));
   return it;
 }

@@ -438,6 +438,7 @@ struct FcgScalars {
   double fsum;     // sum of f over the interior fluid cells
   double neast;    // fluid cells of the outflow column x = W-2
   double nfluid;   // interior fluid cells
+  double zsum;     // sum of the preconditioned residual z over the interior fluid cells
   unsigned maxbits;  // max|r| as float bits
   unsigned pad;
 };
