@@ -319,21 +319,39 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_zsum(const float *__restrict__ z
                                                      FcgPartials *pr) {
   griddep_wait();
   float s = 0.0f;
+  // grid-stride over tiles of 128 x 8 cells, four tiles per pass with
+  // their loads issued together (rows are padded to the pitch, a multiple
+  // of 32 cells, so a float4 / uchar4 at x4 < W stays in the row)
   const int tiles_x = (W + 4 * BX - 1) / (4 * BX), ntiles = tiles_x * ((H + BY - 1) / BY);
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int x4 = ((t % tiles_x) * BX + threadIdx.x) * 4, y = (t / tiles_x) * BY + threadIdx.y;
-    if (x4 >= W || y < 1 || y >= H - 1) continue;
-    const size_t i = (size_t)y * P + x4;
-    if (x4 >= 1 && x4 + 4 <= W - 1) {
-      const float4 a = *reinterpret_cast<const float4 *>(z + i);
-      const uchar4 c = __ldg(reinterpret_cast<const uchar4 *>(code + i));
-      s = s + ((((c.x & 1u) ? a.x : 0.0f) + ((c.y & 1u) ? a.y : 0.0f)) +
-               (((c.z & 1u) ? a.z : 0.0f) + ((c.w & 1u) ? a.w : 0.0f)));
-    } else {
-      for (int j = 0; j < 4; j++) {
-        const int x = x4 + j;
-        if (x >= 1 && x < W - 1 && (__ldg(code + i + j) & 1u)) s = s + z[i + j];
+  const int G = (int)gridDim.x;
+  for (int t0 = blockIdx.x; t0 < ntiles; t0 += 4 * G) {
+    float4 a[4];
+    uchar4 c[4];
+    int xs[4];
+    bool ok[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int t = t0 + u * G;
+      const int x4 = ((t % tiles_x) * BX + threadIdx.x) * 4, y = (t / tiles_x) * BY + threadIdx.y;
+      ok[u] = t < ntiles && x4 < W && y >= 1 && y < H - 1;
+      xs[u] = x4;
+      if (ok[u]) {
+        const size_t i = (size_t)y * P + x4;
+        a[u] = *reinterpret_cast<const float4 *>(z + i);
+        c[u] = __ldg(reinterpret_cast<const uchar4 *>(code + i));
       }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (!ok[u]) continue;
+      const int x4 = xs[u];
+      const float A[4] = {a[u].x, a[u].y, a[u].z, a[u].w};
+      const unsigned C[4] = {c[u].x, c[u].y, c[u].z, c[u].w};
+      float t4[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        t4[j] = (x4 + j >= 1 && x4 + j < W - 1 && (C[j] & 1u)) ? A[j] : 0.0f;
+      s = s + ((t4[0] + t4[1]) + (t4[2] + t4[3]));
     }
   }
   double v[1] = {(double)s};
@@ -358,18 +376,30 @@ __global__ void __launch_bounds__(BX *BY) k_fcg_zq(const float *__restrict__ z,
     sc->dr = 0.0;
   }
   float s = 0.0f;
-  // grid-stride over tiles of 128 x 8 cells: a few blocks per SM, so few
-  // same-address atomics in the final reduction
+  // grid-stride over tiles of 128 x 8 cells, four tiles per pass with
+  // their loads issued together
   const int tiles_x = (W + 4 * BX - 1) / (4 * BX), ntiles = tiles_x * ((H + BY - 1) / BY);
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int x4 = ((t % tiles_x) * BX + threadIdx.x) * 4, y = (t / tiles_x) * BY + threadIdx.y;
-    if (x4 < W && y < H) {
-      const size_t i = (size_t)y * P + x4;
-      const float4 a = *reinterpret_cast<const float4 *>(z + i);
-      const float4 b = *reinterpret_cast<const float4 *>(q + i);
-      // q is 0 outside the interior fluid cells and beyond the width
-      s = s + ((((a.x - zm) * b.x + (a.y - zm) * b.y) + (a.z - zm) * b.z) + (a.w - zm) * b.w);
+  const int G = (int)gridDim.x;
+  for (int t0 = blockIdx.x; t0 < ntiles; t0 += 4 * G) {
+    float4 a[4], b[4];
+    bool ok[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int t = t0 + u * G;
+      const int x4 = ((t % tiles_x) * BX + threadIdx.x) * 4, y = (t / tiles_x) * BY + threadIdx.y;
+      ok[u] = t < ntiles && x4 < W && y < H;
+      if (ok[u]) {
+        const size_t i = (size_t)y * P + x4;
+        a[u] = *reinterpret_cast<const float4 *>(z + i);
+        b[u] = *reinterpret_cast<const float4 *>(q + i);
+      }
     }
+    // q is 0 outside the interior fluid cells and beyond the width
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (ok[u])
+        s = s + ((((a[u].x - zm) * b[u].x + (a[u].y - zm) * b[u].y) + (a[u].z - zm) * b[u].z) +
+                 (a[u].w - zm) * b[u].w);
   }
   double v[1] = {(double)s};
   double *const dst[1] = {&sc->zq};
