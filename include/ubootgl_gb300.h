@@ -72,20 +72,26 @@ enum ubg_field {
  * V-cycles, simulation.cpp:189-190, and never looks at the residual). */
 enum ubg_solver_mode {
   UBG_SOLVE_FIXED = 0,     /* `vcycles` V-cycles (2 = the reference) */
-  UBG_SOLVE_TOLERANCE = 1  /* V-cycles until ||r|| <= tol * ||f|| (FP64 norms over the
-                              interior fluid cells) or max_vcycles.  The solver's
+  UBG_SOLVE_TOLERANCE = 1  /* flexible CG preconditioned by one V-cycle per
+                              iteration until ||r|| <= tol * ||f_c|| (FP64 norms
+                              over the interior fluid cells) or max_vcycles.  The
                               system has zero-gradient edges everywhere and is
-                              singular, so this mode first subtracts the mean
-                              of f over the interior fluid cells: it solves the
-                              compatible part. */
+                              singular; f_c is f with its sum over the fluid cells
+                              moved onto the fluid cells of the outflow column
+                              x = W-2.  The pressure iterate is double-float; a
+                              solve that ends above the residual it started from
+                              keeps its starting pressure.  The solve waits on the
+                              host for its residuals, so a tolerance step is not
+                              captured into a graph. */
 };
 
 /* Precision of the multigrid corrections (extension).  FP32 is the
- * reference's arithmetic.  MIXED_* run an FP32 defect-correction loop
- * (residual, convergence test and p += e in FP32, norms in FP64) whose inner
- * V-cycle stores the error equation in FP16 / BF16 on every level, computes
- * in FP32 registers, and solves the coarse levels (<= 2048 cells) in FP64.
- * In FIXED mode each V-cycle is one correction, and k corrections equal (in
+ * reference's arithmetic.  TOLERANCE mode: the preconditioner's level 0 is
+ * always FP32; MIXED_* store the coarse levels in FP16 / BF16 (scaled by a
+ * power of two found on the device, FP32 arithmetic).  FIXED mode: MIXED_*
+ * run an FP32 defect-correction loop (residual and p += e in FP32) whose
+ * inner V-cycle stores the error equation in FP16 / BF16 on every level and
+ * solves the coarse levels (<= 2048 cells) in FP64; k corrections equal (in
  * exact arithmetic) k V-cycles of the reference started from p with
  * zero-gradient edges. */
 enum ubg_precision { UBG_FP32 = 0, UBG_MIXED_FP16 = 1, UBG_MIXED_BF16 = 2 };
