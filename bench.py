@@ -310,6 +310,10 @@ def run_ours(args):
                    "l2": "inputs larger than L2: step working set %.0f MB > 129 MB"
                          % (working_set_bytes(W, H) / 1e6)},
         "autotune": ({"tail_cells": tune["tail_cells"],
+                      "cluster_top": tune.get("cluster_top"),
+                      "vcycle_us": tune.get("vcycle_us"),
+                      "cluster_trial_us": [t["vcycle_us"] for t in tune.get("trials", [])
+                                           if t.get("what") == "cluster"],
                       "tiles": [(lv["pre"], lv["post"]) for lv in tune["levels"]]}
                      if tune else None),
         "clocks": clk,

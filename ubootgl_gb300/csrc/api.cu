@@ -502,8 +502,11 @@ int ubg_device_info(char *buf, size_t len) {
     UBG_CUDA(cudaGetDevice(&dev));
     cudaDeviceProp p;
     UBG_CUDA(cudaGetDeviceProperties(&p, dev));
-    snprintf(buf, len, "{\"name\": \"%s\", \"sm\": \"%d.%d\", \"sms\": %d, \"mem_gb\": %.1f}", p.name,
-             p.major, p.minor, p.multiProcessorCount, p.totalGlobalMem / 1e9);
+    snprintf(buf, len,
+             "{\"name\": \"%s\", \"sm\": \"%d.%d\", \"sms\": %d, \"mem_gb\": %.1f, "
+             "\"cluster_coarse_solve\": \"%s\"}",
+             p.name, p.major, p.minor, p.multiProcessorCount, p.totalGlobalMem / 1e9,
+             cluster_coarse_solve_status());
     return UBG_OK;
   });
 }

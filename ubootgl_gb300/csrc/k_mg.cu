@@ -18,6 +18,7 @@
 // all red points, then all black points, which is the reference's
 // deterministic schedule.  Every kernel reads one buffer and writes another,
 // so tiles never race on their halos.
+#include <cooperative_groups.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -983,12 +984,32 @@ __device__ __forceinline__ void team_sync(int team) {
 // S: storage of the top level's rhs and result (float, or the 16-bit type of
 // the mixed solver); T: arithmetic and shared-memory type (float, or double
 // for the FP64 coarse solve of the mixed solver).
+// Loads the tail's codes and zeroes its e arrays; level 0's rhs comes from
+// rhs_top (from_global) or is zeroed for its producer to fill.
 template <class S, class T>
-__device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
+__device__ __forceinline__ void tail_load(const TailArgs<S> &a, T *fm, uint8_t *bm,
+                                          bool from_global) {
   using St = Sto<S>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *fm = reinterpret_cast<T *>(smem_raw);
-  uint8_t *bm = smem_raw + (size_t)a.float_words * sizeof(T);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nl = a.nlev;
+  for (int t = 0; t < nl; t++) {
+    const TailLevel &L = a.L[t];
+    for (int y = ty; y < L.h; y += 32)
+      for (int x = tx; x < L.w; x += 32) {
+        int q = y * L.w + x;
+        bm[L.oc + q] = a.code[t][(size_t)y * a.code_pitch[t] + x];
+        fm[L.oe + q] = T(0);
+        if (t == 0)
+          fm[L.orhs + q] = from_global ? (T)St::tof(a.rhs_top[(size_t)y * a.rhs_pitch + x]) : T(0);
+      }
+  }
+}
+
+// The tail's levels on shared memory (fm: arithmetic arrays, bm: codes),
+// with level 0's rhs and zeroed e arrays in place: down, the coarsest level,
+// up.  Block-local barriers only.
+template <class S, class T>
+__device__ __forceinline__ void tail_levels(const TailArgs<S> &a, T *fm, uint8_t *bm) {
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
   const int nl = a.nlev;
   const float ws0 = a.wsum[0], ws1 = a.wsum[1], ws2 = a.wsum[2], ws3 = a.wsum[3], ws4 = a.wsum[4];
@@ -1009,17 +1030,6 @@ __device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
     return TAIL_THREADS;
   };
 
-  for (int t = 0; t < nl; t++) {
-    const TailLevel &L = a.L[t];
-    for (int y = ty; y < L.h; y += 32)
-      for (int x = tx; x < L.w; x += 32) {
-        int q = y * L.w + x;
-        bm[L.oc + q] = a.code[t][(size_t)y * a.code_pitch[t] + x];
-        fm[L.oe + q] = T(0);
-        if (t == 0) fm[L.orhs + q] = (T)St::tof(a.rhs_top[(size_t)y * a.rhs_pitch + x]);
-      }
-  }
-  __syncthreads();
 
   // setZeroGradientBC on level t, plus the corners in ext mode
   auto zero_gradient = [&](int t, int team) {
@@ -1156,6 +1166,18 @@ __device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
     if (a.ext) zero_gradient(t, team);
     sweeps(t, 3, team);
   }
+}
+
+template <class S, class T>
+__device__ __forceinline__ void k_mg_tail_body(const TailArgs<S> &a) {
+  using St = Sto<S>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *fm = reinterpret_cast<T *>(smem_raw);
+  uint8_t *bm = smem_raw + (size_t)a.float_words * sizeof(T);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  tail_load<S, T>(a, fm, bm, true);
+  __syncthreads();
+  tail_levels<S, T>(a, fm, bm);
   __syncthreads();
   const TailLevel &L0 = a.L[0];
   for (int y = ty; y < L0.h; y += 32)
@@ -1175,6 +1197,260 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1)
   griddep_wait();
   if (!table_ok(bs, n, tag, err)) return;
   k_mg_tail_body<float, float>(A[blockIdx.x]);
+}
+
+// ------------------------------------------------ cluster coarse solve
+// The coarse end of the V-cycle from a level of up to ~512x256 cells down,
+// in one launch of a cluster of CT_CTAS thread blocks (the reference's
+// hierarchy, FP32).  Levels cluster_top .. tail_top-1 are split into row
+// bands, one per block, each in its block's shared memory with one ghost
+// row on either side.  After a phase changes the first or last row of a
+// band, the block writes those cells into its neighbours' ghost rows
+// through distributed shared memory, and the cluster barrier makes them
+// visible.  The bands nest: block k owns rows [2b, 2b') of a level when it
+// owns rows [b, b') of the next coarser one (the last block also takes the
+// extra rows of odd heights), so a restriction reads only its band and the
+// ghost row below it, and a prolongation its coarse band and the ghost row
+// above.  The tail's levels (tail_top down) run in block 0 alone, as in the
+// one-block tail kernel.  Every cell goes through the arithmetic of the
+// tiled kernels and the tail, so the results are the same bits.  Each
+// sweep's half only sends the cells of the colour it updated: the
+// neighbour reads only the other colour of its ghost rows in that phase.
+namespace cg = cooperative_groups;
+constexpr int CT_MAXD = 6;
+constexpr int CT_CTAS = 16;
+constexpr size_t CT_SMEM_MAX = 227 * 1024;
+
+struct CtLevel {
+  int w, h, rows;     // level size; local rows per block (largest band + 2)
+  float hh, ihsq, rfac;
+  int oe, orr, orhs;  // float offsets of the local e / r / rhs arrays (rows x w)
+  int oc;             // byte offset of the local codes
+  int band[CT_CTAS + 1];
+  const uint8_t *code;
+  int code_pitch;
+};
+struct CTailArgs {
+  int nd;                    // banded levels
+  CtLevel D[CT_MAXD];
+  int tband[CT_CTAS + 1];    // row bands of the tail's top level (restriction targets)
+  TailArgs<float> tail;      // the tail's levels, run by block 0
+  int tail_fo, tail_bo;      // float / byte offsets of the tail's region
+  int float_words;           // floats before the byte region
+  const float *rhs_top;      // level cluster_top's rhs and result (global)
+  int rhs_pitch;
+  float *e_top;
+  int e_pitch;
+  float wsum[5], rwsum[5];
+};
+
+__global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_constant__ CTailArgs a) {
+  griddep_wait();
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  constexpr int C = CT_CTAS;
+  constexpr int NT = TAIL_THREADS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *fm = reinterpret_cast<float *>(smem_raw);
+  uint8_t *bm = smem_raw + (size_t)a.float_words * sizeof(float);
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const float ws0 = a.wsum[0], ws1 = a.wsum[1], ws2 = a.wsum[2], ws3 = a.wsum[3], ws4 = a.wsum[4];
+  const float rw0 = a.rwsum[0], rw1 = a.rwsum[1], rw2 = a.rwsum[2], rw3 = a.rwsum[3],
+              rw4 = a.rwsum[4];
+  auto DIVW = [&](float x, int k) -> float {
+    const float d = k == 0 ? ws0 : (k == 1 ? ws1 : (k == 2 ? ws2 : (k == 3 ? ws3 : ws4)));
+    const float r = k == 0 ? rw0 : (k == 1 ? rw1 : (k == 2 ? rw2 : (k == 3 ? rw3 : rw4)));
+    return div_rn(x, d, r);
+  };
+
+  // load: codes of the band and ghost rows, zeroed e / r, level 0's rhs
+  for (int d = 0; d < a.nd; d++) {
+    const CtLevel &L = a.D[d];
+    const int y0 = L.band[rank], y1 = L.band[rank + 1], w = L.w, n = (y1 - y0 + 2) * w;
+    for (int k = tid; k < n; k += NT) {
+      const int lr = k / w, x = k - lr * w, y = y0 - 1 + lr;
+      const bool in = y >= 0 && y < L.h;
+      bm[L.oc + k] = in ? L.code[(size_t)y * L.code_pitch + x] : (uint8_t)0;
+      fm[L.oe + k] = 0.0f;
+      fm[L.orr + k] = 0.0f;
+      fm[L.orhs + k] = (d == 0 && y >= y0 && y < y1) ? a.rhs_top[(size_t)y * a.rhs_pitch + x] : 0.0f;
+    }
+  }
+  if (rank == 0) tail_load<float, float>(a.tail, fm + a.tail_fo, bm + a.tail_bo, false);
+  cl.sync();
+
+  // The first / last band row of array `off` of level d into the
+  // neighbours' ghost rows: the cells of colour `color` ((x + y + color)
+  // even), or whole rows for color < 0.
+  auto send_rows = [&](int d, int off, int color, bool first, bool last) {
+    const CtLevel &L = a.D[d];
+    const int y0 = L.band[rank], y1 = L.band[rank + 1], w = L.w;
+    float *arr = fm + off;
+    if (first && rank > 0) {
+      float *dst = cl.map_shared_rank(arr, rank - 1) + (y0 - L.band[rank - 1] + 1) * w;
+      const float *src = arr + w;
+      for (int x = tid; x < w; x += NT)
+        if (color < 0 || ((x + y0 + color) & 1) == 0) dst[x] = src[x];
+    }
+    if (last && rank < C - 1) {
+      float *dst = cl.map_shared_rank(arr, rank + 1);
+      const float *src = arr + (y1 - y0) * w;
+      for (int x = tid; x < w; x += NT)
+        if (color < 0 || ((x + y1 - 1 + color) & 1) == 0) dst[x] = src[x];
+    }
+  };
+
+  // one half-sweep (colour `color`) of level d's band, then the exchange
+  auto dsweep = [&](int d, int color) {
+    const CtLevel &L = a.D[d];
+    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1], hw2 = (w + 1) / 2;
+    float *e = fm + L.oe;
+    const float *f = fm + L.orhs;
+    const uint8_t *c = bm + L.oc;
+    const float hh = L.hh;
+    const int ya = max(y0, 1), yb = min(y1, L.h - 1);
+    const int n = max(yb - ya, 0) * hw2;
+    for (int k = tid; k < n; k += NT) {
+      const int ry = k / hw2, j = k - ry * hw2, y = ya + ry;
+      const int x = 2 * j + ((y + color) & 1);
+      if (x < 1 || x >= w - 1) continue;
+      const int i = (y - y0 + 1) * w + x;
+      const unsigned ci = c[i];
+      const float pw = e[i - 1], pe = e[i + 1], ps = e[i - w], pn = e[i + w], fi = f[i];
+      if (ci == (C_CENTER | C_W | C_E | C_S | C_N))
+        e[i] = ((((pw + pe) + ps) + pn) + fi * hh * hh) * 0.25f;
+      else
+        e[i] = rb_update1<float>(ci, pw, pe, ps, pn, fi, hh);
+    }
+    __syncthreads();
+    send_rows(d, L.oe, color, true, true);
+    cl.sync();
+  };
+
+  // residual of level d's band; the last band row goes to the next block
+  auto dresid = [&](int d) {
+    const CtLevel &L = a.D[d];
+    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1], n = (y1 - y0) * w;
+    const float *e = fm + L.oe, *f = fm + L.orhs;
+    float *r = fm + L.orr;
+    const uint8_t *c = bm + L.oc;
+    const float ihsq = L.ihsq;
+    for (int k = tid; k < n; k += NT) {
+      const int ry = k / w, x = k - ry * w, y = y0 + ry, q = (ry + 1) * w + x;
+      float rv = 0.0f;
+      if (x >= 1 && x < w - 1 && y >= 1 && y < L.h - 1)
+        rv = resid1<float>(c[q], e[q], e[q - 1], e[q + 1], e[q - w], e[q + w], f[q], ihsq);
+      r[q] = rv;
+    }
+    __syncthreads();
+    send_rows(d, L.orr, -1, false, true);
+    cl.sync();
+  };
+
+  // full-weighting restriction of level d's residual into the next level's
+  // rhs: its band (local) or, below the banded levels, the tail's top level
+  // in block 0
+  auto drestrict = [&](int d) {
+    const CtLevel &L = a.D[d];
+    const bool to_tail = d + 1 == a.nd;
+    const int w = L.w, y0 = L.band[rank];
+    const int wc = to_tail ? a.tail.L[0].w : a.D[d + 1].w;
+    const int hc = to_tail ? a.tail.L[0].h : a.D[d + 1].h;
+    const int Y0 = to_tail ? a.tband[rank] : a.D[d + 1].band[rank];
+    const int Y1 = to_tail ? a.tband[rank + 1] : a.D[d + 1].band[rank + 1];
+    float *rc = to_tail ? cl.map_shared_rank(fm + a.tail_fo + a.tail.L[0].orhs, 0)
+                        : fm + a.D[d + 1].orhs;
+    const float *r = fm + L.orr;
+    const float rfac = L.rfac;
+    const int n = (Y1 - Y0) * wc;
+    for (int k = tid; k < n; k += NT) {
+      const int rY = k / wc, X = k - rY * wc, Y = Y0 + rY;
+      if (X < 1 || X >= wc - 1 || Y < 1 || Y >= hc - 1) continue;
+      const float *R0 = r + (2 * Y - y0 + 1) * w + 2 * X;
+      float v = (R0[-w - 1] * 1.0f + R0[-w] * 2.0f) + R0[-w + 1] * 1.0f;
+      v = v + ((R0[-1] * 2.0f + R0[0] * 4.0f) + R0[1] * 2.0f);
+      v = v + ((R0[w - 1] * 1.0f + R0[w] * 2.0f) + R0[w + 1] * 1.0f);
+      v = v * rfac;
+      if (to_tail)
+        rc[Y * wc + X] = v;
+      else
+        rc[(Y - Y0 + 1) * wc + X] = v;
+    }
+    cl.sync();
+  };
+
+  // prolongation of the next level's e onto level d's band, correction,
+  // then whole first / last rows to the neighbours
+  auto dprolong = [&](int d) {
+    const CtLevel &L = a.D[d];
+    const bool from_tail = d + 1 == a.nd;
+    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1], n = (y1 - y0) * w;
+    float *e = fm + L.oe;
+    const uint8_t *c = bm + L.oc;
+    const int wc = from_tail ? a.tail.L[0].w : a.D[d + 1].w;
+    const int Y0 = from_tail ? 0 : a.D[d + 1].band[rank] - 1;
+    const float *ec = from_tail ? cl.map_shared_rank(fm + a.tail_fo + a.tail.L[0].oe, 0)
+                                : fm + a.D[d + 1].oe;
+    const uint8_t *cg_ = from_tail ? a.tail.code[0] : bm + a.D[d + 1].oc;
+    const int cpitch = from_tail ? a.tail.code_pitch[0] : wc;
+    auto E = [&](int xx, int yy) { return ec[(yy - Y0) * wc + xx]; };
+    auto F = [&](int xx, int yy) {
+      return (int)((from_tail ? __ldg(cg_ + (size_t)yy * cpitch + xx)
+                              : cg_[(size_t)(yy - Y0) * cpitch + xx]) &
+                   1u);
+    };
+    for (int k = tid; k < n; k += NT) {
+      const int ry = k / w, x = k - ry * w, y = y0 + ry;
+      if (x < 1 || x >= w - 1 || y < 1 || y >= L.h - 1) continue;
+      const int q = (ry + 1) * w + x;
+      if (!(c[q] & C_CENTER)) continue;
+      const int cx = x >> 1, cy = y >> 1;
+      const bool xo = x & 1, yo = y & 1;
+      float ev;
+      if (!xo && !yo)
+        ev = E(cx, cy);
+      else if (xo && !yo)
+        ev = (x >= w - 2) ? 0.0f : DIVW(E(cx, cy) + E(cx + 1, cy), F(cx, cy) + F(cx + 1, cy));
+      else if (!xo && yo)
+        ev = (y >= L.h - 2) ? 0.0f : DIVW(E(cx, cy) + E(cx, cy + 1), F(cx, cy) + F(cx, cy + 1));
+      else
+        ev = (x >= w - 2 || y >= L.h - 2)
+                 ? 0.0f
+                 : DIVW(((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1),
+                        F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1));
+      e[q] = e[q] + ev;
+    }
+    __syncthreads();
+    send_rows(d, L.oe, -1, true, true);
+    cl.sync();
+  };
+
+  for (int d = 0; d < a.nd; d++) {
+    for (int s = 0; s < 3; s++) {
+      dsweep(d, 1);
+      dsweep(d, 0);
+    }
+    dresid(d);
+    drestrict(d);
+  }
+  if (rank == 0) tail_levels<float, float>(a.tail, fm + a.tail_fo, bm + a.tail_bo);
+  cl.sync();
+  for (int d = a.nd - 1; d >= 0; d--) {
+    dprolong(d);
+    for (int s = 0; s < 3; s++) {
+      dsweep(d, 1);
+      dsweep(d, 0);
+    }
+  }
+  {
+    const CtLevel &L = a.D[0];
+    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1], n = (y1 - y0) * w;
+    for (int k = tid; k < n; k += NT) {
+      const int ry = k / w, x = k - ry * w;
+      a.e_top[(size_t)(y0 + ry) * a.e_pitch + x] = fm[L.oe + (ry + 1) * w + x];
+    }
+  }
+  cl.sync();  // no block leaves while another may still read its memory
 }
 
 // ------------------------------------------------------------ launches
@@ -1248,6 +1524,9 @@ void set_multi_attr() {
 // Sets the shared-memory attributes of every smoother and tail kernel, once
 // per process (function-local static initialisation is thread-safe; the
 // server's worker thread and the caller's threads may race here).
+bool g_ctail_ok = false;  // a cluster of the coarse solve fits this device
+char g_ctail_why[160] = "not probed";
+
 static void set_all_kernel_attributes() {
   set_multi_attr<112, 50, 8>();
   set_multi_attr<48, 16, 8>();
@@ -1280,6 +1559,40 @@ static void set_all_kernel_attributes() {
   set_smem_attr<48, 16, 8, true, 256, float, __nv_bfloat16, true>();
   set_tail_attr<__half, float>();
   set_tail_attr<__nv_bfloat16, float>();
+  // the cluster coarse solve: 16 blocks of up to 227 KB each, if the device
+  // can hold such a cluster (else the launches per level are used)
+  g_ctail_ok = false;
+  cudaError_t e1 = cudaFuncSetAttribute(k_mg_ctail, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)CT_SMEM_MAX);
+  cudaError_t e2 = e1 == cudaSuccess
+                       ? cudaFuncSetAttribute(k_mg_ctail,
+                                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1)
+                       : e1;
+  if (e2 != cudaSuccess) {
+    snprintf(g_ctail_why, sizeof(g_ctail_why), "attributes: %s", cudaGetErrorString(e2));
+  } else {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(CT_CTAS);
+    cfg.blockDim = dim3(32, TAIL_THREADS / 32);
+    cfg.dynamicSmemBytes = CT_SMEM_MAX;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CT_CTAS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    cudaError_t e3 = cudaOccupancyMaxActiveClusters(&nclusters, k_mg_ctail, &cfg);
+    g_ctail_ok = e3 == cudaSuccess && nclusters >= 1;
+    if (g_ctail_ok)
+      snprintf(g_ctail_why, sizeof(g_ctail_why), "available (%d clusters of %d blocks)",
+               nclusters, CT_CTAS);
+    else
+      snprintf(g_ctail_why, sizeof(g_ctail_why), "occupancy: %s, %d clusters",
+               cudaGetErrorString(e3), nclusters);
+  }
+  cudaGetLastError();
 }
 
 void init_kernel_attributes() {
@@ -1444,10 +1757,131 @@ void run_tail(MgHier &mg, int lt, cudaStream_t st) {
   run_tail_t<float, float>(mg, lt, mg.lv[lt].rhs, mg.lv[lt].e[0], nullptr, st);
 }
 
+// Arguments of the cluster coarse solve from level ct (banded levels ct ..
+// tail_top-1, the tail below); false if the hierarchy or the shared memory
+// does not allow it.
+bool ctail_args(MgHier &mg, int ct, CTailArgs &a, size_t &smem) {
+  const int T = mg.tail_top;
+  if (mg.ext || ct < 1 || T < 2 || ct >= T || T - ct > CT_MAXD || T > mg_coarsest(mg))
+    return false;
+  constexpr int C = CT_CTAS;
+  if (mg.lv[T].h < C) return false;
+  for (int l = ct; l < T; l++)
+    if (mg.lv[l + 1].h != mg.lv[l].h / 2 || mg.lv[l + 1].w != mg.lv[l].w / 2) return false;
+  a = CTailArgs{};
+  size_t tsm = 0;
+  try {
+    a.tail = tail_args<float, float>(mg, T, nullptr, nullptr, nullptr, &tsm);
+  } catch (const ArgError &) {
+    return false;
+  }
+  a.nd = T - ct;
+  // bands: the tail's top level split evenly, each finer level's bands the
+  // doubled ones (the last block takes the extra rows of odd heights)
+  const int hT = mg.lv[T].h;
+  for (int k = 0; k < C; k++) a.tband[k] = (int)(((long long)k * hT) / C);
+  a.tband[C] = hT;
+  const int *next = a.tband;
+  for (int d = a.nd - 1; d >= 0; d--) {
+    CtLevel &D = a.D[d];
+    const MgLevel &L = mg.lv[ct + d];
+    for (int k = 0; k < C; k++) D.band[k] = 2 * next[k];
+    D.band[C] = L.h;
+    int rows = 0;
+    for (int k = 0; k < C; k++) {
+      if (D.band[k + 1] <= D.band[k]) return false;
+      rows = std::max(rows, D.band[k + 1] - D.band[k]);
+    }
+    D.rows = rows + 2;
+    D.w = L.w;
+    D.h = L.h;
+    D.hh = L.hh;
+    D.ihsq = 1.0f / L.hh / L.hh;
+    D.rfac = 1.0f / 16.0f;
+    D.code = L.code;
+    D.code_pitch = L.pitch;
+    next = D.band;
+  }
+  size_t fo = 0, bo = 0;
+  for (int d = 0; d < a.nd; d++) {
+    CtLevel &D = a.D[d];
+    const size_t n = (size_t)D.rows * D.w;
+    D.oe = (int)fo;
+    fo += (n + 3) / 4 * 4;
+    D.orr = (int)fo;
+    fo += (n + 3) / 4 * 4;
+    D.orhs = (int)fo;
+    fo += (n + 3) / 4 * 4;
+    D.oc = (int)bo;
+    bo += (n + 15) / 16 * 16;
+  }
+  a.tail_fo = (int)fo;
+  fo += (size_t)a.tail.float_words;
+  a.tail_bo = (int)bo;
+  bo += tsm - (size_t)a.tail.float_words * sizeof(float);
+  a.float_words = (int)fo;
+  smem = fo * sizeof(float) + bo;
+  if (smem > CT_SMEM_MAX) return false;
+  const MgLevel &top = mg.lv[ct];
+  a.rhs_top = top.rhs;
+  a.rhs_pitch = top.pitch;
+  a.e_top = top.e[0];
+  a.e_pitch = top.pitch;
+  for (int k = 0; k < 5; k++) {
+    a.wsum[k] = (float)((double)(float)k + 0.0001);
+    a.rwsum[k] = 1.0f / a.wsum[k];
+  }
+  return true;
+}
+
+// The lowest level from which the cluster coarse solve covers the rest of
+// the V-cycle, or -1.
+int choose_cluster(MgHier &mg) {
+  init_kernel_attributes();
+  if (!g_ctail_ok) return -1;
+  int best = -1;
+  for (int ct = mg.tail_top - 1; ct >= 1; ct--) {
+    CTailArgs a;
+    size_t smem = 0;
+    if (!ctail_args(mg, ct, a, smem)) break;
+    best = ct;
+  }
+  return best;
+}
+
+void run_ctail(MgHier &mg, int ct, cudaStream_t st) {
+  ProfScope ps_(KC_TAIL, st);
+  CTailArgs a;
+  size_t smem = 0;
+  if (!ctail_args(mg, ct, a, smem)) throw ArgError("cluster coarse solve: hierarchy does not fit");
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(CT_CTAS);
+  cfg.blockDim = dim3(32, TAIL_THREADS / 32);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CT_CTAS;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+  UBG_CUDA(cudaLaunchKernelEx(&cfg, k_mg_ctail, a));
+  UBG_LAUNCH_CHECK();
+  g_stats.launches++;
+}
+
 // MG::solveLevel, pressure_solver.cpp:201-248.
 void solve_level(MgHier &mg, std::vector<int> &cur, int l, bool zgbc, cudaStream_t st) {
   bool bc = zgbc && l == 0;
   MgLevel &L = mg.lv[l];
+  if (l >= 1 && l == mg.cluster_top) {
+    run_ctail(mg, l, st);
+    cur[l] = 0;
+    return;
+  }
   if (l >= 1 && l == mg.tail_top) {
     run_tail(mg, l, st);
     cur[l] = 0;
@@ -1848,6 +2282,11 @@ int choose_tail(const std::vector<MgLevel> &lv, int max_cells, size_t elem_bytes
 
 }  // namespace
 
+const char *cluster_coarse_solve_status() {
+  init_kernel_attributes();
+  return g_ctail_why;
+}
+
 namespace {
 std::vector<MgLevel> level_shapes(int W, int H, float h0) {
   int cw = W, ch = H;
@@ -1904,6 +2343,13 @@ void mg_bind(MgHier &mg, int W, int H, float h0, void *arena, size_t bytes) {
   mg.tail_top_fp64 = choose_tail(lv, 128, 8);
   mg.lv = lv;
   mg.levels = (int)lv.size();
+  // the cluster coarse solve from two levels above the tail (the autotuner
+  // measured that choice fastest at 1024x512, 4096x2048 and 8192x4096;
+  // from larger levels its 16 blocks have too much work per phase)
+  {
+    const int lowest = choose_cluster(mg);
+    mg.cluster_top = lowest >= 1 ? std::max(lowest, mg.tail_top - 2) : -1;
+  }
   mg.arena = nullptr;  // not owned
   mg.arena_bytes = bytes;
   mg.cur0 = 0;
@@ -2020,7 +2466,7 @@ double time_ms(EvPair &ev, cudaStream_t st, int warm, int reps, F &&f) {
 // simulations of one size (the members of a batch, the sessions of a
 // server) share the first one's trials.
 struct TuneChoice {
-  int tail_cells = 0, tail_top = 0;
+  int tail_cells = 0, tail_top = 0, cluster_top = -1;
   std::vector<int> pre, post;
 };
 std::mutex g_tune_mu;
@@ -2036,6 +2482,7 @@ void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
     if (it != g_tune_cache.end() && (int)it->second.pre.size() == nl) {
       mg.tail_cells = it->second.tail_cells;
       mg.tail_top = it->second.tail_top;
+      mg.cluster_top = it->second.cluster_top;
       for (int l = 0; l < nl; l++) {
         mg.lv[l].tile_pre = it->second.pre[l];
         mg.lv[l].tile_post = it->second.post[l];
@@ -2043,8 +2490,8 @@ void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
       if (report) {
         char buf[160];
         snprintf(buf, sizeof(buf),
-                 "{\"cached\": true, \"tail_cells\": %d, \"tail_top\": %d, \"levels\": [",
-                 mg.tail_cells, mg.tail_top);
+                 "{\"cached\": true, \"tail_cells\": %d, \"tail_top\": %d, \"cluster_top\": %d, \"levels\": [",
+                 mg.tail_cells, mg.tail_top, mg.cluster_top);
         std::string rep = buf;
         const int last = (mg.tail_top >= 1 ? mg.tail_top : nl - 1) - 1;
         for (int l = 0; l <= std::min(last, nl - 3); l++) {
@@ -2090,6 +2537,9 @@ void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
     cudaGraphExecDestroy(ge);
     return 1e3 * ms;
   };
+  // the tail and the tiles are tuned with launches per level; the cluster
+  // coarse solve is tried last
+  mg.cluster_top = -1;
   std::string rep = "{\"trials\": [";
   bool first = true;
   auto note = [&](const char *what, int level, const char *choice, double us) {
@@ -2142,12 +2592,27 @@ void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
       slot = keep;
     }
   }
+  {
+    // every feasible first level of the cluster coarse solve
+    const int lowest = choose_cluster(mg);
+    int keep = -1;
+    for (int ct = mg.tail_top - 1; lowest >= 1 && ct >= lowest; ct--) {
+      mg.cluster_top = ct;
+      double t = vcycle_us();
+      note("cluster", ct, "on", t);
+      if (t < best) {
+        best = t;
+        keep = ct;
+      }
+    }
+    mg.cluster_top = keep;
+  }
   UBG_CUDA(cudaMemcpyAsync(L0.e[c0], saved, pbytes, cudaMemcpyDeviceToDevice, st));
   UBG_CUDA(cudaStreamSynchronize(st));
   cudaFree(saved);
   char buf[256];
-  snprintf(buf, sizeof(buf), "], \"vcycle_us\": %.2f, \"tail_cells\": %d, \"tail_top\": %d, \"levels\": [",
-           best, mg.tail_cells, mg.tail_top);
+  snprintf(buf, sizeof(buf), "], \"vcycle_us\": %.2f, \"tail_cells\": %d, \"tail_top\": %d, \"cluster_top\": %d, \"levels\": [",
+           best, mg.tail_cells, mg.tail_top, mg.cluster_top);
   rep += buf;
   for (int l = 0; l <= std::min(last, nl - 3); l++) {
     const MgLevel &L = mg.lv[l];
@@ -2161,6 +2626,7 @@ void mg_autotune(MgHier &mg, cudaStream_t st, std::string *report) {
   TuneChoice tc;
   tc.tail_cells = mg.tail_cells;
   tc.tail_top = mg.tail_top;
+  tc.cluster_top = mg.cluster_top;
   for (int l = 0; l < nl; l++) {
     tc.pre.push_back(mg.lv[l].tile_pre);
     tc.post.push_back(mg.lv[l].tile_post);

@@ -322,6 +322,10 @@ struct MgHier {
   int tail_top = -1;             // first level solved by the one-CTA tail kernel
   int tail_cells = 2048;         // largest top level the tail takes (autotuned)
   int tail_top_fp64 = -1;        // the same for the mixed solver's FP64 tail
+  // First level of the cluster coarse solve (levels cluster_top ..
+  // tail_top-1 in row bands over a thread-block cluster, the tail's levels
+  // in its first CTA; one launch), or -1: launches per level.
+  int cluster_top = -1;
   void *arena = nullptr;
   size_t arena_bytes = 0;
   double *norm = nullptr;        // device scalar for residual norms
@@ -334,6 +338,8 @@ struct MgHier {
   int ncoarse = 5;
 };
 inline int mg_coarsest(const MgHier &mg) { return mg.ext ? mg.levels - 1 : mg.levels - 2; }
+// Whether the cluster coarse solve can run on this device, and why not.
+const char *cluster_coarse_solve_status();
 
 // Times the candidate smoother tiles of every level and the tail sizes on
 // this hierarchy's own arrays (state preserved: trials write only scratch
