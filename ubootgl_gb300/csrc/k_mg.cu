@@ -1262,19 +1262,29 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
     const float r = k == 0 ? rw0 : (k == 1 ? rw1 : (k == 2 ? rw2 : (k == 3 ? rw3 : rw4)));
     return div_rn(x, d, r);
   };
+  // (row, 32-column segment) items to warps, columns to lanes: one
+  // division per warp item instead of one per cell
+  const int wid = tid >> 5, lane = tid & 31;
+  auto for_cells = [&](int nrows, int ncols, auto &&fn) {
+    const int nseg = (ncols + 31) >> 5;
+    for (int it = wid; it < nrows * nseg; it += NT / 32) {
+      const int r = it / nseg, c = (it - r * nseg) * 32 + lane;
+      if (c < ncols) fn(r, c);
+    }
+  };
 
   // load: codes of the band and ghost rows, zeroed e / r, level 0's rhs
   for (int d = 0; d < a.nd; d++) {
     const CtLevel &L = a.D[d];
-    const int y0 = L.band[rank], y1 = L.band[rank + 1], w = L.w, n = (y1 - y0 + 2) * w;
-    for (int k = tid; k < n; k += NT) {
-      const int lr = k / w, x = k - lr * w, y = y0 - 1 + lr;
+    const int y0 = L.band[rank], y1 = L.band[rank + 1], w = L.w;
+    for_cells(y1 - y0 + 2, w, [&](int lr, int x) {
+      const int y = y0 - 1 + lr, k = lr * w + x;
       const bool in = y >= 0 && y < L.h;
       bm[L.oc + k] = in ? L.code[(size_t)y * L.code_pitch + x] : (uint8_t)0;
       fm[L.oe + k] = 0.0f;
       fm[L.orr + k] = 0.0f;
       fm[L.orhs + k] = (d == 0 && y >= y0 && y < y1) ? a.rhs_top[(size_t)y * a.rhs_pitch + x] : 0.0f;
-    }
+    });
   }
   if (rank == 0) tail_load<float, float>(a.tail, fm + a.tail_fo, bm + a.tail_bo, false);
   cl.sync();
@@ -1309,11 +1319,10 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
     const uint8_t *c = bm + L.oc;
     const float hh = L.hh;
     const int ya = max(y0, 1), yb = min(y1, L.h - 1);
-    const int n = max(yb - ya, 0) * hw2;
-    for (int k = tid; k < n; k += NT) {
-      const int ry = k / hw2, j = k - ry * hw2, y = ya + ry;
+    for_cells(max(yb - ya, 0), hw2, [&](int ry, int j) {
+      const int y = ya + ry;
       const int x = 2 * j + ((y + color) & 1);
-      if (x < 1 || x >= w - 1) continue;
+      if (x < 1 || x >= w - 1) return;
       const int i = (y - y0 + 1) * w + x;
       const unsigned ci = c[i];
       const float pw = e[i - 1], pe = e[i + 1], ps = e[i - w], pn = e[i + w], fi = f[i];
@@ -1321,7 +1330,7 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
         e[i] = ((((pw + pe) + ps) + pn) + fi * hh * hh) * 0.25f;
       else
         e[i] = rb_update1<float>(ci, pw, pe, ps, pn, fi, hh);
-    }
+    });
     __syncthreads();
     send_rows(d, L.oe, color, true, true);
     cl.sync();
@@ -1330,18 +1339,18 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
   // residual of level d's band; the last band row goes to the next block
   auto dresid = [&](int d) {
     const CtLevel &L = a.D[d];
-    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1], n = (y1 - y0) * w;
+    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1];
     const float *e = fm + L.oe, *f = fm + L.orhs;
     float *r = fm + L.orr;
     const uint8_t *c = bm + L.oc;
     const float ihsq = L.ihsq;
-    for (int k = tid; k < n; k += NT) {
-      const int ry = k / w, x = k - ry * w, y = y0 + ry, q = (ry + 1) * w + x;
+    for_cells(y1 - y0, w, [&](int ry, int x) {
+      const int y = y0 + ry, q = (ry + 1) * w + x;
       float rv = 0.0f;
       if (x >= 1 && x < w - 1 && y >= 1 && y < L.h - 1)
         rv = resid1<float>(c[q], e[q], e[q - 1], e[q + 1], e[q - w], e[q + w], f[q], ihsq);
       r[q] = rv;
-    }
+    });
     __syncthreads();
     send_rows(d, L.orr, -1, false, true);
     cl.sync();
@@ -1362,10 +1371,9 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
                         : fm + a.D[d + 1].orhs;
     const float *r = fm + L.orr;
     const float rfac = L.rfac;
-    const int n = (Y1 - Y0) * wc;
-    for (int k = tid; k < n; k += NT) {
-      const int rY = k / wc, X = k - rY * wc, Y = Y0 + rY;
-      if (X < 1 || X >= wc - 1 || Y < 1 || Y >= hc - 1) continue;
+    for_cells(Y1 - Y0, wc, [&](int rY, int X) {
+      const int Y = Y0 + rY;
+      if (X < 1 || X >= wc - 1 || Y < 1 || Y >= hc - 1) return;
       const float *R0 = r + (2 * Y - y0 + 1) * w + 2 * X;
       float v = (R0[-w - 1] * 1.0f + R0[-w] * 2.0f) + R0[-w + 1] * 1.0f;
       v = v + ((R0[-1] * 2.0f + R0[0] * 4.0f) + R0[1] * 2.0f);
@@ -1375,7 +1383,7 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
         rc[Y * wc + X] = v;
       else
         rc[(Y - Y0 + 1) * wc + X] = v;
-    }
+    });
     cl.sync();
   };
 
@@ -1384,7 +1392,7 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
   auto dprolong = [&](int d) {
     const CtLevel &L = a.D[d];
     const bool from_tail = d + 1 == a.nd;
-    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1], n = (y1 - y0) * w;
+    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1];
     float *e = fm + L.oe;
     const uint8_t *c = bm + L.oc;
     const int wc = from_tail ? a.tail.L[0].w : a.D[d + 1].w;
@@ -1399,11 +1407,11 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
                               : cg_[(size_t)(yy - Y0) * cpitch + xx]) &
                    1u);
     };
-    for (int k = tid; k < n; k += NT) {
-      const int ry = k / w, x = k - ry * w, y = y0 + ry;
-      if (x < 1 || x >= w - 1 || y < 1 || y >= L.h - 1) continue;
+    for_cells(y1 - y0, w, [&](int ry, int x) {
+      const int y = y0 + ry;
+      if (x < 1 || x >= w - 1 || y < 1 || y >= L.h - 1) return;
       const int q = (ry + 1) * w + x;
-      if (!(c[q] & C_CENTER)) continue;
+      if (!(c[q] & C_CENTER)) return;
       const int cx = x >> 1, cy = y >> 1;
       const bool xo = x & 1, yo = y & 1;
       float ev;
@@ -1419,7 +1427,7 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
                  : DIVW(((E(cx, cy) + E(cx + 1, cy + 1)) + E(cx + 1, cy)) + E(cx, cy + 1),
                         F(cx, cy) + F(cx + 1, cy + 1) + F(cx + 1, cy) + F(cx, cy + 1));
       e[q] = e[q] + ev;
-    }
+    });
     __syncthreads();
     send_rows(d, L.oe, -1, true, true);
     cl.sync();
@@ -1444,11 +1452,10 @@ __global__ void __launch_bounds__(TAIL_THREADS, 1) k_mg_ctail(const __grid_const
   }
   {
     const CtLevel &L = a.D[0];
-    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1], n = (y1 - y0) * w;
-    for (int k = tid; k < n; k += NT) {
-      const int ry = k / w, x = k - ry * w;
+    const int w = L.w, y0 = L.band[rank], y1 = L.band[rank + 1];
+    for_cells(y1 - y0, w, [&](int ry, int x) {
       a.e_top[(size_t)(y0 + ry) * a.e_pitch + x] = fm[L.oe + (ry + 1) * w + x];
-    }
+    });
   }
   cl.sync();  // no block leaves while another may still read its memory
 }
