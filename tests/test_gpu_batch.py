@@ -82,11 +82,23 @@ def test_batch_host_dt_accum_and_member_steps(lib):
 
 
 def test_autotune_bit_identical(lib):
+    """The autotuner's choices (tiles, tail size, the cluster coarse solve's
+    first level or the launches per level) give the same bits as the
+    defaults (which start the cluster coarse solve two levels above the
+    tail where the device can hold the cluster)."""
+    import ctypes as C
+    import json
+    buf = C.create_string_buffer(1024)
+    assert lib.ubg_device_info(buf, len(buf)) == 0
+    cluster = json.loads(buf.value.decode())["cluster_coarse_solve"].startswith("available")
     a = build(1024, 512, 77)
     b = build(1024, 512, 77)
     rep = b.autotune()
     assert rep["levels"] and "tail_cells" in rep and rep["vcycle_us"] > 0
     assert all(t["vcycle_us"] > 0 for t in rep["trials"])
+    assert "cluster_top" in rep
+    if cluster:  # every feasible first level was timed
+        assert sum(t["what"] == "cluster" for t in rep["trials"]) >= 2
     for _ in range(3):
         a.step_cfl(0.5)
         b.step_cfl(0.5)
