@@ -277,6 +277,9 @@ def run_ours(args):
         for prec in ("fp16", "bf16"):
             modes["fixed_" + prec] = time_mode(L, lib, flag, vx, vy, prec, args.mode_steps,
                                                args.warmup, dev)
+        # the advection option: bilinearSample for the back-trace
+        modes["fp32_bilinear_advect"] = time_mode(L, lib, flag, vx, vy, "fp32", args.mode_steps,
+                                                  args.warmup, dev, advect="bilinear")
 
     # ---- batched uneven instances and the served stream (extensions)
     batched, served = {}, {}
@@ -389,16 +392,17 @@ def time_tolerance(L, lib, flag, vx, vy, precision, steps, warmup, dev, tol):
             "fields_finite": finite}
 
 
-def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev):
+def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev, advect="bicubic"):
     """Whole steps with the mixed-precision pressure solver (2 defect
-    corrections, each one 16-bit V-cycle, in the captured step graph), timed
+    corrections, each one 16-bit V-cycle, in the captured step graph), or
+    with precision "fp32" the plain step with the advection option, timed
     with CUDA events on the simulation's stream."""
     import ctypes as C
     import torch
     from ubootgl_gb300.simulation import Simulation
     H, W = flag.shape
     sim = Simulation(flag, 1.0, 1e-4)
-    sim.set_options(solver_mode=L.SOLVE_FIXED, vcycles=2, precision=precision)
+    sim.set_options(solver_mode=L.SOLVE_FIXED, vcycles=2, precision=precision, advect=advect)
     for n, a in (("vx", vx), ("vy", vy), ("vx_back", vx), ("vy_back", vy)):
         sim.set(n, a)
     stream = C.c_void_p()
@@ -430,8 +434,10 @@ def time_mode(L, lib, flag, vx, vy, precision, steps, warmup, dev):
             for k, v in sorted(classes.items(), key=lambda kv: -kv[1][0])}
     return {"value": round(W * H * steps / (ms / 1e3) / 1e6, 2), "unit": "Mcell-steps/s",
             "ms_per_step": round(ms / steps, 5), "steps": steps, "kernels": kern,
-            "solver": "2 FP32 defect corrections, 16-bit (%s) V-cycle, FP64 norms and coarse "
-                      "solve" % precision, "fields_finite": finite}
+            "solver": ("2 FP32 defect corrections, 16-bit (%s) V-cycle, FP64 norms and coarse "
+                       "solve" % precision if precision != "fp32"
+                       else "the reference's 2 FP32 V-cycles"),
+            "advect": advect, "fields_finite": finite}
 
 
 def batch_bench(L, lib, n, steps, warmup, precision, seed=11, wmin=128, wmax=2048):

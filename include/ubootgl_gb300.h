@@ -103,6 +103,8 @@ typedef struct ubg_options {
   int max_vcycles;    /* TOLERANCE mode: cap, default 100 */
   int precision;      /* ubg_precision, default UBG_FP32 */
   int use_graph;      /* capture the step into a CUDA graph, default 1 */
+  int advect_bilinear; /* 1: advection samples with bilinearSample (interpolators.hpp:11-27)
+                          instead of bicubicSample (extension); default 0, the reference */
 } ubg_options;
 
 typedef struct ubg_sim ubg_sim;

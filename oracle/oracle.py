@@ -73,6 +73,9 @@ def _bind_port(lib):
         g("rbgs").argtypes = [P, P, P, C.c_int, C.c_int, ct, ct]
         g("residual").restype = C.c_double
         g("residual").argtypes = [P, P, P, P, C.c_int, C.c_int, ct]
+        g("set_advect_bilinear").argtypes = [C.c_void_p, C.c_int]
+        g("bilinear_sample").restype = ct
+        g("bilinear_sample").argtypes = [P, C.c_int, C.c_int, ct, ct]
         g("advect_mask_vx").argtypes = [P, C.c_int, C.c_int, C.c_int]
         g("advect_mask_vy").argtypes = [P, C.c_int, C.c_int, C.c_int]
     lib.ubo_omp_set_threads.argtypes = [C.c_int]
@@ -226,6 +229,11 @@ class PortSim:
     def add_sink(self, x, y, z):
         self._fn("add_sink")(self.h_, x, y, z)
 
+    def set_advect_bilinear(self, on=True):
+        """Advection samples with bilinearSample instead of bicubicSample
+        (the extension's option; the reference advects bicubically)."""
+        self._fn("set_advect_bilinear")(self.h_, 1 if on else 0)
+
     def levels(self):
         return self._fn("mg_levels")(self.h_)
 
@@ -371,6 +379,14 @@ def bilinear_sample(grid, cx, cy):
     vm1 = v1 + (v2 - v1) * sx
     vm2 = v3 + (v4 - v3) * sx
     return vm1 + (vm2 - vm1) * sy
+
+
+def port_bilinear_sample(grid, cx, cy):
+    """The C restatement's bilinearSample (the advection option's sampler)."""
+    g = np.ascontiguousarray(grid, dtype=np.float32)
+    gh, gw = g.shape
+    return np.float32(port_lib().ubo_f_bilinear_sample(_fp(g, C.c_float), gw, gh,
+                                                       np.float32(cx), np.float32(cy)))
 
 
 def bilinear_scatter(grid, cx, cy, v):

@@ -53,6 +53,7 @@ typedef struct {
   MG_T mg;
   int nsinks;
   REAL sinks[UBO_MAXSINKS][3];
+  int bilinear; /* advection samples: 0 bicubicSample (the reference), 1 bilinearSample */
 } SIM_T;
 
 static REAL *FN(alloc)(size_t n) {
@@ -470,6 +471,29 @@ static inline REAL FN(bicubic)(const REAL *g, int gw, int gh, REAL cx, REAL cy) 
   return FN(cr_dot)(wx, col[0], col[1], col[2], col[3]);
 }
 
+/* bilinearSample, interpolators.hpp:11-27: clamp to [0, size - 1.1]
+ * (glm::clamp = min(max(c, lo), hi)), truncate, interpolate along x, then
+ * along y.  The advection option samples with it instead of bicubicSample
+ * (extension; the reference advects bicubically). */
+static inline REAL FN(bilinear)(const REAL *g, int gw, int gh, REAL cx, REAL cy) {
+  REAL hx = (REAL)gw - (REAL)1.1f, hy = (REAL)gh - (REAL)1.1f;
+  cx = cx < (REAL)0.0 ? (REAL)0.0 : cx;
+  cx = hx < cx ? hx : cx;
+  cy = cy < (REAL)0.0 ? (REAL)0.0 : cy;
+  cy = hy < cy ? hy : cy;
+  int ix = (int)cx, iy = (int)cy;
+  REAL sx = cx - (REAL)ix, sy = cy - (REAL)iy;
+  REAL v1 = AT(g, gw, ix, iy), v2 = AT(g, gw, ix + 1, iy);
+  REAL v3 = AT(g, gw, ix, iy + 1), v4 = AT(g, gw, ix + 1, iy + 1);
+  REAL vm1 = v1 + (v2 - v1) * sx;
+  REAL vm2 = v3 + (v4 - v3) * sx;
+  return vm1 + (vm2 - vm1) * sy;
+}
+REAL FN(bilinear_sample)(const REAL *g, int gw, int gh, REAL cx, REAL cy) {
+  return FN(bilinear)(g, gw, gh, cx, cy);
+}
+void FN(set_advect_bilinear)(SIM_T *s, int on) { s->bilinear = on ? 1 : 0; }
+
 /* Whether the reference advects face x of row y.  The x loops run in chunks
  * of 8 from x = 1 while x < width-8 (simulation.cpp:248, 300), so the last
  * columns are never advected, and a chunk is skipped when none of its 8
@@ -491,14 +515,18 @@ int FN(advect_mask_vy)(const REAL *flag, int W, int x, int y) {
 }
 
 /* advect, simulation.cpp:241-354: RK2 back-trace per face, three bicubic
- * samples, result * face mask into the back buffer, then swap both grids.
+ * samples (bilinear with the advection option), result * face mask into the
+ * back buffer, then swap both grids.
  * The vy loop runs over the vx rows 1..H-2 (simulation.cpp:247), so it also
  * writes vy row H-2; setVBCs overwrites that row afterwards.  The vx average
  * of the vy loop reads flat index x+1+y*(W-1), which for x = W-2 is element 0
  * of the next row; REF_VX reproduces that. */
 #define REF_VX(vx, W, x, y) ((vx)[(size_t)(y) * (size_t)((W)-1) + (size_t)(x)])
+#define SAMPLE(g, gw, gh, cx, cy) \
+  (bil ? FN(bilinear)(g, gw, gh, cx, cy) : FN(bicubic)(g, gw, gh, cx, cy))
 void FN(advect)(SIM_T *s) {
   int W = s->W, H = s->H;
+  const int bil = s->bilinear;
   const REAL *flag = s->flag;
   REAL ih = (REAL)1.0 / s->h;
   REAL chalf = (REAL)0.5 * s->dt * ih;
@@ -518,11 +546,11 @@ void FN(advect)(SIM_T *s) {
                  (REAL)0.25;
       REAL midx = posx - vx1 * chalf;
       REAL midy = posy - vy1 * chalf;
-      REAL vx2 = FN(bicubic)(vx, vxw, vxh, midx - (REAL)0.5, midy);
-      REAL vy2 = FN(bicubic)(vy, vyw, vyh, midx, midy - (REAL)0.5);
+      REAL vx2 = SAMPLE(vx, vxw, vxh, midx - (REAL)0.5, midy);
+      REAL vy2 = SAMPLE(vy, vyw, vyh, midx, midy - (REAL)0.5);
       REAL endx = posx - vx2 * cfull;
       REAL endy = posy - vy2 * cfull;
-      REAL v = FN(bicubic)(vx, vxw, vxh, endx - (REAL)0.5, endy);
+      REAL v = SAMPLE(vx, vxw, vxh, endx - (REAL)0.5, endy);
       AT(vxo, vxw, x, y) = v * AT(flag, W, x, y) * AT(flag, W, x + 1, y);
     }
     for (int x = 1; x < vyw - 1; x++) {
@@ -534,11 +562,11 @@ void FN(advect)(SIM_T *s) {
                  (REAL)0.25;
       REAL midx = posx - vx1 * chalf;
       REAL midy = posy - vy1 * chalf;
-      REAL vx2 = FN(bicubic)(vx, vxw, vxh, midx - (REAL)0.5, midy);
-      REAL vy2 = FN(bicubic)(vy, vyw, vyh, midx, midy - (REAL)0.5);
+      REAL vx2 = SAMPLE(vx, vxw, vxh, midx - (REAL)0.5, midy);
+      REAL vy2 = SAMPLE(vy, vyw, vyh, midx, midy - (REAL)0.5);
       REAL endx = posx - vx2 * cfull;
       REAL endy = posy - vy2 * cfull;
-      REAL v = FN(bicubic)(vy, vyw, vyh, endx, endy - (REAL)0.5);
+      REAL v = SAMPLE(vy, vyw, vyh, endx, endy - (REAL)0.5);
       AT(vyo, vyw, x, y) = v * AT(flag, W, x, y) * AT(flag, W, x, y + 1);
     }
   }
@@ -546,6 +574,7 @@ void FN(advect)(SIM_T *s) {
   s->fx = 1 - s->fx;
   s->fy = 1 - s->fy;
 }
+#undef SAMPLE
 
 /* -------------------------------------------------------------- projection */
 /* project, simulation.cpp:164-208: divergence into f, explosion sinks, two

@@ -75,3 +75,16 @@ def test_shift_map_restatement_invariants():
     assert not f["p"][0].any() and not f["vx"][0].any()
     u = np.float32(np.float32(0.07) * np.float32(H)) / np.float32(1.0 + (H - 2))
     assert np.array_equal(f["vx"][1:-1, 0], np.full(H - 2, u, np.float32))
+
+
+def test_bilinear_advection_sampler_matches_pinned_restatement():
+    """The C restatement's bilinearSample (the advection option's sampler)
+    equals the numpy restatement that is pinned against the reference build
+    above, bit for bit, on points inside and outside the clamp range."""
+    rng = np.random.default_rng(7)
+    g = rng.standard_normal((37, 53)).astype(np.float32)
+    for _ in range(5000):
+        cx, cy = rng.uniform(-3.0, 60.0), rng.uniform(-3.0, 45.0)
+        a = O.port_bilinear_sample(g, cx, cy)
+        b = O.bilinear_sample(g, cx, cy)
+        assert a == b, (cx, cy, a, b)

@@ -26,7 +26,8 @@ class UbgError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("solver_mode", C.c_int), ("vcycles", C.c_int), ("tol", C.c_float),
-                ("max_vcycles", C.c_int), ("precision", C.c_int), ("use_graph", C.c_int)]
+                ("max_vcycles", C.c_int), ("precision", C.c_int), ("use_graph", C.c_int),
+                ("advect_bilinear", C.c_int)]
 
 
 class ServeStats(C.Structure):

@@ -535,6 +535,7 @@ int ubg_default_options(ubg_options *o) {
   o->max_vcycles = 100;
   o->precision = UBG_FP32;
   o->use_graph = 1;
+  o->advect_bilinear = 0;
   return UBG_OK;
 }
 
@@ -622,6 +623,7 @@ int ubg_set_options(ubg_sim *s, const ubg_options *o) {
         o->precision != UBG_MIXED_BF16)
       throw ArgError("precision");
     if (o->solver_mode == UBG_SOLVE_TOLERANCE && !(o->tol > 0.0f)) throw ArgError("tol must be > 0");
+    if (o->advect_bilinear != 0 && o->advect_bilinear != 1) throw ArgError("advect_bilinear");
     UBG_CUDA(cudaStreamSynchronize(s->st));
     if (o->solver_mode == UBG_SOLVE_TOLERANCE) {
       // flexible CG over the tolerance hierarchy; the fixed-mode 16-bit
@@ -637,6 +639,7 @@ int ubg_set_options(ubg_sim *s, const ubg_options *o) {
         mg_low_alloc(s->lo, s->mg, o->precision);
     }
     s->opt = *o;
+    s->v.advect_bilinear = o->advect_bilinear;
     s->gen++;
     return UBG_OK;
   });
@@ -1639,7 +1642,8 @@ FusedStepper::~FusedStepper() {
 
 bool FusedStepper::eligible(const ubg_sim *s) {
   return s->opt.precision == UBG_FP32 && s->opt.solver_mode == UBG_SOLVE_FIXED &&
-         s->opt.vcycles >= 1 && s->mg.tail_top >= 1 && s->sinks.empty() && !s->prof;
+         !s->opt.advect_bilinear && s->opt.vcycles >= 1 && s->mg.tail_top >= 1 &&
+         s->sinks.empty() && !s->prof;
 }
 
 int FusedStepper::group(const ubg_sim *s) { return s->opt.vcycles; }

@@ -396,6 +396,40 @@ __device__ __forceinline__ float bicubic_win(const Win &wn, const float *__restr
   return bicubic16(g + (size_t)(iy - 1) * P + (ix - 1), P, sx, sy);
 }
 
+// bilinearSample (interpolators.hpp:11-27) for the advection option: clamp
+// to [0, size - 1.1] (glm::clamp = min(max(c, lo), hi)), truncate,
+// interpolate along x, then along y; the four values from the shared-memory
+// window when they lie inside, else from global memory.
+template <int SW, int SH>
+__device__ __forceinline__ float bilinear_win(const Win &wn, const float *__restrict__ g, int P,
+                                              int gw, int gh, float cx, float cy) {
+  const float hx = (float)gw - 1.1f, hy = (float)gh - 1.1f;
+  cx = cx < 0.0f ? 0.0f : cx;
+  cx = hx < cx ? hx : cx;
+  cy = cy < 0.0f ? 0.0f : cy;
+  cy = hy < cy ? hy : cy;
+  const int ix = (int)cx, iy = (int)cy;
+  const float sx = cx - (float)ix, sy = cy - (float)iy;
+  const int lx = ix - wn.sx0, ly = iy - wn.sy0;
+  float v1, v2, v3, v4;
+  if (lx >= 0 && lx + 1 < SW && ly >= 0 && ly + 1 < SH) {
+    const float *b = wn.s + ly * SW + lx;
+    v1 = b[0];
+    v2 = b[1];
+    v3 = b[SW];
+    v4 = b[SW + 1];
+  } else {
+    const float *b = g + (size_t)iy * P + ix;
+    v1 = b[0];
+    v2 = b[1];
+    v3 = b[P];
+    v4 = b[P + 1];
+  }
+  const float vm1 = v1 + (v2 - v1) * sx;
+  const float vm2 = v3 + (v4 - v3) * sx;
+  return vm1 + (vm2 - vm1) * sy;
+}
+
 // advect, simulation.cpp:241-354.  A block handles the vx and vy faces of a
 // 64 x 16 tile of cells; both velocity components are staged in shared
 // memory with a 4-cell halo, which holds every stencil of a back-trace that
@@ -404,6 +438,8 @@ __device__ __forceinline__ float bicubic_win(const Win &wn, const float *__restr
 constexpr int AD_TX = 64, AD_TY = 16, AD_H = 4;
 constexpr int AD_SW = AD_TX + 2 * AD_H, AD_SH = AD_TY + 2 * AD_H;
 
+// BIL: the advection option's bilinearSample instead of bicubicSample.
+template <bool BIL>
 __device__ __forceinline__ void k_advect_body(VelBufs v, int srcx, int srcy,
                                                 const StepScalars *__restrict__ sc, const int bx, const int by, const int bz) {
   __shared__ __align__(16) float sxv[AD_SH * AD_SW];
@@ -457,6 +493,13 @@ __device__ __forceinline__ void k_advect_body(VelBufs v, int srcx, int srcy,
   auto SX = [&](int x, int y) { return sxv[(y - sy0) * AD_SW + (x - sx0)]; };
   auto SY = [&](int x, int y) { return syv[(y - sy0) * AD_SW + (x - sx0)]; };
   float *outx = pick(v.vx, 1 - srcx), *outy = pick(v.vy, 1 - srcy);
+  auto SAMPLE = [&](const Win &wn, const float *__restrict__ g, int P_, int gw, int gh, float cx,
+                    float cy) {
+    if constexpr (BIL)
+      return bilinear_win<AD_SW, AD_SH>(wn, g, P_, gw, gh, cx, cy);
+    else
+      return bicubic_win<AD_SW, AD_SH>(wn, g, P_, gw, gh, cx, cy);
+  };
   for (int i = tid; i < AD_TX * AD_TY; i += 256) {
     int ty = i / AD_TX, tx = i - ty * AD_TX;
     int x = X0 + tx, y = Y0 + ty;
@@ -470,11 +513,11 @@ __device__ __forceinline__ void k_advect_body(VelBufs v, int srcx, int srcy,
         float vy1 = ((SY(x, y) + SY(x, y - 1)) + (SY(x + 1, y) + SY(x + 1, y - 1))) * 0.25f;
         float midx = posx - vx1 * chalf;
         float midy = posy - vy1 * chalf;
-        float vx2 = bicubic_win<AD_SW, AD_SH>(wx, vx, P, W - 1, H, midx - 0.5f, midy);
-        float vy2 = bicubic_win<AD_SW, AD_SH>(wy, vy, P, W, H - 1, midx, midy - 0.5f);
+        float vx2 = SAMPLE(wx, vx, P, W - 1, H, midx - 0.5f, midy);
+        float vy2 = SAMPLE(wy, vy, P, W, H - 1, midx, midy - 0.5f);
         float endx = posx - vx2 * cfull;
         float endy = posy - vy2 * cfull;
-        float r = bicubic_win<AD_SW, AD_SH>(wx, vx, P, W - 1, H, endx - 0.5f, endy);
+        float r = SAMPLE(wx, vx, P, W - 1, H, endx - 0.5f, endy);
         outx[(size_t)y * P + x] = (k & FC_M) ? r : 0.0f;
       }
     }
@@ -491,20 +534,21 @@ __device__ __forceinline__ void k_advect_body(VelBufs v, int srcx, int srcy,
         float vx1 = ((SX(x, y) + SX(x, y - 1)) + (a2 + a3)) * 0.25f;
         float midx = posx - vx1 * chalf;
         float midy = posy - vy1 * chalf;
-        float vx2 = bicubic_win<AD_SW, AD_SH>(wx, vx, P, W - 1, H, midx - 0.5f, midy);
-        float vy2 = bicubic_win<AD_SW, AD_SH>(wy, vy, P, W, H - 1, midx, midy - 0.5f);
+        float vx2 = SAMPLE(wx, vx, P, W - 1, H, midx - 0.5f, midy);
+        float vy2 = SAMPLE(wy, vy, P, W, H - 1, midx, midy - 0.5f);
         float endx = posx - vx2 * cfull;
         float endy = posy - vy2 * cfull;
-        float r = bicubic_win<AD_SW, AD_SH>(wy, vy, P, W, H - 1, endx, endy - 0.5f);
+        float r = SAMPLE(wy, vy, P, W, H - 1, endx, endy - 0.5f);
         outy[(size_t)y * P + x] = (k & FC_M) ? r : 0.0f;
       }
     }
   }
 }
+template <bool BIL>
 __global__ void __launch_bounds__(256) k_advect(VelBufs v, int srcx, int srcy,
                                                 const StepScalars *__restrict__ sc) {
   griddep_wait();
-  k_advect_body(v, srcx, srcy, sc, blockIdx.x, blockIdx.y, blockIdx.z);
+  k_advect_body<BIL>(v, srcx, srcy, sc, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ------------------------------------------------------------- divergence
@@ -754,7 +798,8 @@ __global__ void __launch_bounds__(256) k_advect_m(const AdvectM *__restrict__ A,
   const int m = member_of(bs, n);
   const AdvectM a = A[m];
   const int l = (int)blockIdx.x - __ldg(bs + m);
-  k_advect_body(a.v, a.srcx, a.srcy, a.sc, l % a.gx, l / a.gx, 0);
+  // fused members advect bicubically (the bilinear option is not fused)
+  k_advect_body<false>(a.v, a.srcx, a.srcy, a.sc, l % a.gx, l / a.gx, 0);
 }
 __global__ void __launch_bounds__(256) k_divergence_m(const DivergenceM *__restrict__ A, const int *__restrict__ bs, int n,
                unsigned tag, unsigned *err) {
@@ -828,7 +873,10 @@ void launch_diffuse_sweep(const VelBufs &v, int srcx, int srcy, const StepScalar
 void launch_advect(const VelBufs &v, int srcx, int srcy, const StepScalars *sc, cudaStream_t st) {
   ProfScope ps_(KC_ADVECT, st);
   dim3 grid((v.W + AD_TX - 1) / AD_TX, (v.H + AD_TY - 1) / AD_TY);
-  launch_pdl(k_advect, grid, dim3(BX, BY), 0, st, v, srcx, srcy, sc);
+  if (v.advect_bilinear)
+    launch_pdl(k_advect<true>, grid, dim3(BX, BY), 0, st, v, srcx, srcy, sc);
+  else
+    launch_pdl(k_advect<false>, grid, dim3(BX, BY), 0, st, v, srcx, srcy, sc);
   UBG_LAUNCH_CHECK();
   g_stats.launches++;
 }

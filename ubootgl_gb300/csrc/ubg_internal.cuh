@@ -104,6 +104,7 @@ struct VelBufs {
   // the four diffusion neighbour terms in the reference's order, FC_A = the
   // reference's advection loop covers this face.
   const uint8_t *cx, *cy;
+  int advect_bilinear;  // advection option: bilinearSample instead of bicubicSample
 };
 constexpr unsigned FC_M = 1, FC_T1 = 2, FC_T2 = 4, FC_T3 = 8, FC_T4 = 16, FC_A = 32;
 // Buffer f of a pair, chosen without indexing the array: a run-time index

@@ -62,9 +62,10 @@ class Simulation:
 
     # ------------------------------------------------------------ options
     def set_options(self, solver_mode=None, vcycles=None, tol=None, max_vcycles=None,
-                    use_graph=None, precision=None):
+                    use_graph=None, precision=None, advect=None):
         """Solver options (extension).  precision: "fp32", "fp16" or "bf16"
-        (the mixed-precision defect-correction solver)."""
+        (the mixed-precision defect-correction solver).  advect: "bicubic"
+        (the reference) or "bilinear" (bilinearSample for the back-trace)."""
         o = L.Options()
         L.check(self._lib.ubg_default_options(C.byref(o)))
         cur = getattr(self, "_opts", None)
@@ -83,6 +84,8 @@ class Simulation:
             o.max_vcycles = max_vcycles
         if use_graph is not None:
             o.use_graph = int(use_graph)
+        if advect is not None:
+            o.advect_bilinear = {"bicubic": 0, "bilinear": 1}[advect]
         L.check(self._lib.ubg_set_options(self._h, C.byref(o)))
         self._opts = o
 
