@@ -17,9 +17,11 @@
 // d, q and the preconditioner output z are FP32; stencil sums add their
 // rounding errors back (TwoSum); dot products and norms are FP32 per thread
 // and FP64 across threads, combined in a fixed order (the same bits on
-// every run).  The V-cycle runs its level 0
-// in FP32 and its coarse levels in FP32, FP16 or BF16 (ubg_options
-// precision).
+// every run).  The mean of z over the interior fluid cells is taken out
+// of every search direction (the constant the V-cycle leaves in z would
+// otherwise turn the dot products into rounding noise).  The V-cycle runs
+// its level 0 in FP32 and its coarse levels in FP32, FP16 or BF16
+// (ubg_options precision).
 //
 // Compatibility: the system is singular (constants on each connected fluid
 // region), and f sums to the net flux through the domain edges, which is

@@ -11,6 +11,9 @@
 //              to the next level (calculateResidualField + restrict,
 //              pressure_solver.cpp:91-132) without writing the fine residual.
 //  k_mg_tail   the coarse end of the V-cycle in one CTA, in shared memory.
+//  k_mg_ctail  the coarse end from a larger level down in one launch of a
+//              16-CTA cluster: row bands with ghost rows exchanged through
+//              distributed shared memory, the tail's levels in CTA 0.
 //  k_residual  the residual field and its squared L2 norm.
 //  k_coarsen   MG::updateFields (pressure_solver.hpp:34-57), integer exact.
 //
